@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Benchmark of the per-frame particle physics step on GB300.
+
+Metric: particle-steps/s (particles x frames / s).  Workload: 1,000,000
+particles on a jittered lattice in a 1920x1080 box, cell size 1, extended
+physics (3x3-cell neighbourhood, 4 Jacobi iterations, gravity 0.1 px/frame^2,
+walls, velocity clamp 1).  A step is one frame: solve + rebin.
+
+  value    device-timed frames, state resident in HBM, L2 flushed (a
+           256 MiB write) before every timed frame; CUDA events on the
+           library's stream around each frame
+  e2e      the same metric through the C ABI with pinned host buffers:
+           every step uploads the particles (wrach_set_particles: H2D and
+           the device re-pack), runs one frame and reads the frame back
+           (wrach_read: D2H of positions, velocities and the table)
+  roofline the dominant kernel's algorithmic bytes / its mean CUDA-event
+           duration, against the measured HBM copy bandwidth
+
+`--impl reference` times the reference's CPU path (the oracle port of the
+shader crate, all host threads) on the same workload and metric.
+Multi-GPU: one independent replica per rank (the single-world step does not
+shard), value = all ranks' particle-steps / the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PUBLISHED_PARTICLE_STEPS = 39.0e6  # README.md:14-18 of the reference: ~39 fps at 1M particles
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "particle-steps/s at 1M particles (plain CUDA step)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=4000)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--e2e-steps", type=int, default=50)
+    p.add_argument("--profile-frames", type=int, default=10)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    return p.parse_args()
+
+
+def workload():
+    from wrach_gb300 import workloads
+    dims, pos, vel = workloads.lattice()
+    cfg = dict(cell_size=1, mode=1, iterations=4, gravity=0.1)
+    desc = {"workload": "lattice-1M", "particles": int(len(pos)), "box": list(dims),
+            "cell_size": 1, "physics": "extended (3x3 cells, 4 Jacobi iterations)",
+            "gravity": 0.1, "init": "jittered lattice 1334x750 sites, jitter U(-0.25,0.25), vel N(0,1), seed 0"}
+    return dims, pos, vel, cfg, desc
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
+    FIELDS = ("index,timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def stop(self):
+        if not self.proc:
+            return
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 10:
+                continue
+            try:
+                sm.append(float(parts[2]))
+                mx = float(parts[3])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[6:10]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(dims, pos, vel, cfg, seconds):
+    """The oracle (C port of the reference's shader crate), all host threads,
+    on a bounded number of frames of the same workload."""
+    from oracle import oracle as O
+    w = O.world(dims[0], dims[1], cfg["cell_size"])
+    ph = O.extended_physics(cfg["iterations"], cfg["gravity"]) if cfg["mode"] else O.reference_physics()
+    table, p, v = O.pack(w, pos, vel, O.max_particles_per_frame(w))
+    t0 = time.perf_counter()
+    table, p, v, _ = O.step(w, ph, table, p, v, 1)
+    one = time.perf_counter() - t0
+    frames = max(1, min(200, int(seconds / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    O.step(w, ph, table, p, v, frames)
+    dt = time.perf_counter() - t0
+    return {"value": len(pos) * frames / dt, "unit": "particle-steps/s", "cores": O.num_threads(),
+            "kind": "port", "sample": "%d frames of the %d-particle workload (%.1f s)" % (frames, len(pos), dt)}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    dims, pos, vel, cfg, desc = workload()
+    from oracle import oracle as O
+    w = O.world(dims[0], dims[1], cfg["cell_size"])
+    ph = O.extended_physics(cfg["iterations"], cfg["gravity"])
+    table, p, v = O.pack(w, pos, vel, O.max_particles_per_frame(w))
+    # each step is a bounded sample: one frame of the full workload
+    for _ in range(min(args.warmup, 3)):
+        table, p, v, _ = O.step(w, ph, table, p, v, 1)
+    steps = max(1, min(args.steps, 20))
+    t0 = time.perf_counter()
+    table, p, v, _ = O.step(w, ph, table, p, v, steps)
+    dt = time.perf_counter() - t0
+    value = len(pos) * steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": min(args.warmup, 3),
+            "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": value / PUBLISHED_PARTICLE_STEPS, "dtype": "f32",
+            "data": "synthetic", "config": desc,
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": O.num_threads(),
+                             "kind": "port",
+                             "sample": "%d frames of the full workload on the host cores" % steps},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# algorithmic bytes of each launch of a frame (n particles, c cells)
+def launch_bytes(kind, n, c):
+    if kind == "jacobi":
+        return 20 * n + 4 * c       # q in + q out + cell_of, table once
+    if kind == "jacobi_final":
+        return 40 * n + 4 * c       # q, vel, cell_of in; pos, vel, key out
+    if kind == "solve_reference":
+        return 36 * n + 4 * c       # pos, vel in; pos, vel, key out
+    if kind == "rebin":
+        return 40 * n + 8 * c       # key, pos, vel in; pos, vel, cell_of out; table in + out
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import wrach_gb300 as W
+    W.build()
+    dims, pos, vel, cfg, desc = workload()
+    n = len(pos)
+    sim = W.Simulation(W.WrachConfig(dimensions=dims, device=local, **cfg))
+    sim.add_particles(pos, vel)
+    cells = sim.cells()
+    stream = torch.cuda.ExternalStream(sim.stream, device=torch.device("cuda", local))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+
+    for _ in range(args.warmup):
+        flush_l2()
+        sim.step(1)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local).start()
+    time.sleep(0.25)
+    barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    l0 = sim.kernel_launches
+    for k in range(args.steps):
+        flush_l2()
+        starts[k].record(stream)
+        sim.step(1)
+        ends[k].record(stream)
+    barrier()
+    launches = sim.kernel_launches - l0
+    clocks.stop()
+    dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    t = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = n * args.steps * world / (max_ms / 1000.0)
+
+    # per-kernel durations of eager frames (L2 flushed before each)
+    kinds = (["jacobi"] * (cfg["iterations"] - 1) + ["jacobi_final"] if cfg["mode"] else
+             ["solve_reference"]) + ["rebin"]
+    prof = np.zeros(len(kinds))
+    for _ in range(args.profile_frames):
+        flush_l2()
+        prof += np.array(sim.profile_frame())
+    prof /= args.profile_frames
+    per_kind = {}
+    for k, ms in zip(kinds, prof):
+        per_kind.setdefault(k, []).append(ms)
+    dom = max(per_kind, key=lambda k: sum(per_kind[k]))
+    dom_ms = statistics.mean(per_kind[dom])
+    peak, peak_kind = measured_peak()
+    achieved = launch_bytes(dom, n, cells) / (dom_ms / 1000.0) / 1e9
+    step_bytes = 32 * n + 8 * cells
+    kernels = {k: {"launches_per_step": len(v), "mean_ms": statistics.mean(v),
+                   "gbs": launch_bytes(k, n, cells) / (statistics.mean(v) / 1000.0) / 1e9}
+               for k, v in per_kind.items()}
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        cap = sim.capacity()
+        h_pos = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
+        h_vel = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
+        h_pos[:] = pos
+        h_vel[:] = vel
+        o_pos = torch.empty((cap, 2), dtype=torch.float32, pin_memory=True).numpy()
+        o_vel = torch.empty((cap, 2), dtype=torch.float32, pin_memory=True).numpy()
+        o_idx = torch.empty(cells + 2, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+        for _ in range(2):
+            sim.set_particles(h_pos, h_vel)
+            sim.step(1)
+            sim.read(out=(o_pos, o_vel, o_idx))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            sim.set_particles(h_pos, h_vel)
+            sim.step(1)
+            sim.read(out=(o_pos, o_vel, o_idx))
+        barrier()
+        dt = time.perf_counter() - t0
+        tt = torch.tensor([dt], dtype=torch.float64, device="cuda")
+        if world > 1:
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e = {"value": n * args.e2e_steps * world / float(tt.item()), "unit": "particle-steps/s",
+               "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n + 4 * (cells + 1),
+               "steps": args.e2e_steps,
+               "ms_per_step": 1000.0 * float(tt.item()) / args.e2e_steps}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": value / PUBLISHED_PARTICLE_STEPS, "dtype": "f32", "data": "synthetic",
+        "config": dict(desc, l2="flushed before every timed frame (256 MiB write), flush not timed",
+                       parallelism="replicas" if world > 1 else "single GPU"),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None,
+                     "algorithmic_bytes_per_launch": launch_bytes(dom, n, cells)},
+        "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
+                          "achieved": step_bytes / (max_ms / args.steps / 1000.0) / 1e9,
+                          "frac": step_bytes / (max_ms / args.steps / 1000.0) / 1e9 / peak},
+        "kernels": kernels,
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "e2e": e2e,
+        "flags": sim.flags(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(dims, pos, vel, cfg, args.cpu_seconds)
+    sim.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,175 @@
+/*
+ * wrach.h -- C ABI of the GB300 (sm_103a) CUDA implementation of wrach's
+ * per-frame particle physics step.
+ *
+ * This boundary replaces the reference's `WrachAPI` surface
+ * (runners/api/src/lib.rs:17-88) and the wgpu compute pipeline behind it
+ * (runners/bevy/src/compute/builder.rs:24-92, runners/bevy/src/plugin/
+ * build.rs:88-158).  Plain pointers and sizes only; every call returns a
+ * status code (WRACH_OK == 0) where the reference panics.
+ *
+ * Threading: a context is owned by one thread at a time (the reference's
+ * `&mut self`).  All device work of a context runs in order on the context's
+ * own CUDA stream; wrach_read and wrach_sync block until it is done.
+ *
+ * Data layout (the reference's, runners/bevy/src/spatial_bin.rs:20-33):
+ *   positions, velocities: `capacity` float pairs (x, y), in cell order,
+ *     zero past particles_in_frame_count;
+ *   indices: grid cells + 2 u32, indices[0] = 0, indices[c + 1] = first
+ *     particle of cell c, indices[cells + 1] = particles_in_frame_count.
+ */
+#ifndef WRACH_H
+#define WRACH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WRACH_OK 0
+#define WRACH_ERR_INVALID_ARGUMENT 1 /* null pointer, zero size, bad enum */
+#define WRACH_ERR_CAPACITY 2         /* more particles than the frame holds */
+#define WRACH_ERR_CUDA 3             /* a CUDA call failed; see last_error */
+#define WRACH_ERR_OUT_OF_MEMORY 4    /* device allocation failed */
+#define WRACH_ERR_DEVICE 5           /* a device-side check fired (flags) */
+#define WRACH_ERR_UNSUPPORTED 6      /* no sm_103a device / feature absent */
+
+/* Physics modes. */
+#define WRACH_MODE_REFERENCE 0u /* the reference's same-cell sweep */
+#define WRACH_MODE_EXTENDED 1u  /* 3x3-cell Jacobi iterations + gravity */
+
+/* Sticky device flags (wrach_flags). */
+#define WRACH_FLAG_OUT_OF_GRID 1u /* a key was clamped into the grid */
+#define WRACH_FLAG_NAN 2u         /* a non-finite position was binned */
+#define WRACH_FLAG_TIMEOUT 4u     /* a bounded device wait gave up */
+#define WRACH_FLAG_GENERAL_SORT 8u /* a frame needed the general re-sort */
+
+/* The reference's 32-byte shader uniform, field for field
+ * (runners/bevy/src/config_shader.rs:15-29, shaders/shared/src/lib.rs:19-31,
+ * assets/shaders/types.wgsl:3-15). */
+typedef struct WrachWorldSettings {
+  float view_dimensions[2];
+  float view_anchor[2];
+  uint32_t grid_dimensions[2];
+  uint32_t cell_size;
+  uint32_t particles_in_frame_count;
+} WrachWorldSettings;
+
+/* WrachConfig (runners/bevy/src/config_app.rs:10-36) plus the physics knobs
+ * the reference hard-codes (shaders/physics/src/particles.rs:18,
+ * particle.rs:74, cell.rs:29-30). */
+typedef struct WrachConfig {
+  float width;             /* dimensions.0 (default 480) */
+  float height;            /* dimensions.1 (default 352) */
+  float anchor_x;          /* view_anchor (always 0 in the reference) */
+  float anchor_y;
+  uint32_t cell_size;      /* default 3 (shaders/shared/src/lib.rs:34) */
+  uint32_t mode;           /* WRACH_MODE_* (default REFERENCE) */
+  uint32_t iterations;     /* EXTENDED only (default 4) */
+  float gravity;           /* EXTENDED only, px/frame^2 (default 0) */
+  float min_distance;      /* default 1.0 */
+  float max_velocity;      /* default 1.0 */
+  uint32_t cell_capacity;  /* REFERENCE only, default 9 */
+  uint32_t capacity;       /* 0 = max_particles_per_frame of the grid */
+  int32_t device;          /* CUDA ordinal (default 0) */
+  uint32_t reserved[7];
+} WrachConfig;
+
+typedef struct WrachContext WrachContext;
+
+/* Defaults of WrachConfig::default() (config_app.rs:23-36). */
+int wrach_config_default(WrachConfig *config);
+
+/* WrachAPI::new + PhysicsComputeWorker::build (runners/api/src/lib.rs:30-45,
+ * runners/bevy/src/compute/builder.rs:24-92): sizes the grid from the
+ * viewport (spatial_bin.rs:68-95) and allocates the device buffers. */
+int wrach_create(const WrachConfig *config, WrachContext **out);
+
+/* Many independent worlds stepped together.  `dims` holds 2*nworlds floats
+ * (width, height per world); every other setting comes from `config`.
+ * World w's data is addressed with the `world` argument of the calls below.
+ * No counterpart in the reference (one world per app). */
+int wrach_create_batch(const WrachConfig *config, uint32_t nworlds,
+                       const float *dims, WrachContext **out);
+
+int wrach_destroy(WrachContext *ctx);
+
+/* WrachAPI::add_particles / WrachState::add_particles
+ * (runners/api/src/lib.rs:78-81, runners/bevy/src/state.rs:90-101): appends
+ * n particles (host arrays of n float pairs) to the world's store and re-packs
+ * the whole store into the frame on the device: the cell-ordered layout of
+ * SpatialBin::create_packed_data (spatial_bin.rs:103-149), insertion order
+ * inside a cell, particles outside the viewport grid kept in the store but
+ * left out of the frame.  Like the reference, a re-pack restarts the frame
+ * from the store's particles. */
+int wrach_add_particles(WrachContext *ctx, uint32_t world, const float *pos,
+                        const float *vel, uint32_t n);
+
+/* Replaces the world's store with these n particles and re-packs the frame
+ * from them (ParticleStore::add_particles_to_cell followed by
+ * create_packed_data, runners/bevy/src/particle_store.rs:62-65,103-149,
+ * for the whole store at once). */
+int wrach_set_particles(WrachContext *ctx, uint32_t world, const float *pos,
+                        const float *vel, uint32_t n);
+
+/* As wrach_add_particles with device-resident input arrays. */
+int wrach_add_particles_device(WrachContext *ctx, uint32_t world,
+                               const float *d_pos, const float *d_vel,
+                               uint32_t n);
+
+/* nsteps frames of the physics pass list (builder.rs:86-89): solve, count,
+ * scan, pack.  Asynchronous on the context's stream. */
+int wrach_step(WrachContext *ctx, uint32_t nsteps);
+
+/* WrachAPI::tick's readback (runners/bevy/src/plugin/build.rs:135-158,
+ * runners/api/src/lib.rs:58-74): copies the world's frame into host arrays.
+ * positions/velocities take 2*capacity floats, indices cells+2 u32; any of
+ * the three may be NULL.  `capacity` must be at least the world's frame
+ * capacity (wrach_capacity).  Blocks until the copies are done. */
+int wrach_read(WrachContext *ctx, uint32_t world, float *positions,
+               float *velocities, uint32_t *indices, uint32_t capacity);
+
+/* WrachAPI::tick (runners/api/src/lib.rs:49-52): one step then a read. */
+int wrach_tick(WrachContext *ctx, uint32_t world, float *positions,
+               float *velocities, uint32_t *indices, uint32_t capacity);
+
+/* Settings of a world (the uniform, with particles_in_frame_count). */
+int wrach_get_settings(WrachContext *ctx, uint32_t world,
+                       WrachWorldSettings *out);
+
+/* ParticleStore::max_particles_per_frame (particle_store.rs:116-133) for a
+ * grid of `cells` cells of size `cell_size`. */
+uint32_t wrach_max_particles_per_frame(uint32_t cells, uint32_t cell_size);
+
+/* The frame capacity of a world (the length of its readback arrays). */
+uint32_t wrach_capacity(WrachContext *ctx, uint32_t world);
+uint32_t wrach_num_worlds(WrachContext *ctx);
+
+int wrach_sync(WrachContext *ctx);
+
+/* Sticky device flags (WRACH_FLAG_*) seen since create; blocks. */
+int wrach_flags(WrachContext *ctx, uint32_t *flags);
+
+/* The last error message of the context ("" if none). */
+const char *wrach_last_error(WrachContext *ctx);
+
+/* Runs one frame eagerly with a CUDA event between its kernel launches and
+ * writes each launch's duration in milliseconds to ms[0 .. *count - 1]
+ * (launch order: the solve launches, then the rebin).  Blocks.  No
+ * counterpart in the reference (which has no GPU timers). */
+int wrach_profile_frame(WrachContext *ctx, float *ms, uint32_t cap,
+                        uint32_t *count);
+
+/* Number of kernel launches issued by this context since create. */
+uint64_t wrach_kernel_launches(WrachContext *ctx);
+
+/* The CUDA stream the context runs on (a cudaStream_t). */
+void *wrach_stream(WrachContext *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,241 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Binning (cell keys, the cell-start table, the sorted order) and the physics
+are compared bit for bit: both sides compute in IEEE binary32 without FMA
+contraction, with correctly rounded sqrt and division, in the same order.
+"""
+import numpy as np
+import pytest
+
+from tests.helpers import (assert_frame_equal, frame_stats, make_sim, oracle_physics,
+                           same_bits)
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_both(W, O, dims, cs, pos, vel, mode, steps, iterations=4, gravity=0.0, capacity=0):
+    sim = make_sim(W, dims, cs, mode, iterations, gravity, capacity)
+    try:
+        cap = sim.capacity()
+        w = O.world(dims[0], dims[1], cs)
+        ph = oracle_physics(O, mode, iterations, gravity)
+        sim.add_particles(pos, vel)
+        ref = O.pack(w, pos, vel, capacity=cap)
+        assert_frame_equal(sim.read_frame(), ref, "upload")
+        done = 0
+        for target in steps:
+            sim.step(target - done)
+            ref = O.step(w, ph, ref[0], ref[1], ref[2], target - done)[:3]
+            done = target
+            assert_frame_equal(sim.read_frame(), ref, "after %d steps" % target)
+        return sim.flags()
+    finally:
+        sim.close()
+
+
+def _field(seed, n, dims, vel_sigma, outside=0.0):
+    rng = np.random.default_rng(seed)
+    lo = np.array([-outside, -outside])
+    hi = np.array(dims, np.float64) + outside
+    pos = rng.uniform(lo, hi, size=(n, 2)).astype(np.float32)
+    vel = rng.normal(0, vel_sigma, size=(n, 2)).astype(np.float32)
+    return pos, vel
+
+
+def test_upload_binning_edge_values(W, O):
+    dims, cs = (30.0, 20.0), 3
+    pos, vel = _field(1, 400, dims, 0.5, outside=8.0)
+    special = np.array([[0.0, 0.0], [30.0, 20.0], [-0.0, 5.0], [-1e-45, 3.0], [29.999998, 19.999998],
+                        [np.nan, 1.0], [1.0, np.nan], [np.inf, 1.0], [-np.inf, 2.0], [3.0, 3.0],
+                        [2.9999998, 3.0000002], [33.0, 20.9], [32.999996, 1.0], [1e30, -1e30]],
+                       np.float32)
+    pos = np.concatenate([pos, special])
+    vel = np.concatenate([vel, np.ones_like(special)])
+    sim = make_sim(W, dims, cs)
+    try:
+        sim.add_particles(pos, vel)
+        ref = O.pack(O.world(*dims, cs), pos, vel, capacity=sim.capacity())
+        assert_frame_equal(sim.read_frame(), ref, "upload")
+        s = sim.settings()
+        assert list(s.grid_dimensions) == [11, 7]
+        assert s.particles_in_frame_count == len(ref[1])
+    finally:
+        sim.close()
+
+
+def test_upload_empty_and_repack_store(W, O):
+    dims, cs = (40.0, 40.0), 3
+    a_pos, a_vel = _field(2, 300, dims, 0.3)
+    b_pos, b_vel = _field(3, 200, dims, 0.3, outside=5.0)
+    sim = make_sim(W, dims, cs)
+    try:
+        sim.add_particles(np.zeros((0, 2), np.float32), np.zeros((0, 2), np.float32))
+        p, v, t = sim.read_frame()
+        assert len(p) == 0 and not t.any()
+        sim.add_particles(a_pos, a_vel)
+        sim.step(3)
+        # like the reference, a second add re-packs the whole store
+        # (runners/bevy/src/state.rs:90-101): the frame restarts from it
+        sim.add_particles(b_pos, b_vel)
+        ref = O.pack(O.world(*dims, cs), np.concatenate([a_pos, b_pos]),
+                     np.concatenate([a_vel, b_vel]), capacity=sim.capacity())
+        assert_frame_equal(sim.read_frame(), ref, "repack")
+    finally:
+        sim.close()
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_reference_mode_bit_exact(W, O, seed):
+    # dense enough that cells overflow the capacity of 9 (cell.rs:79-95)
+    dims, cs = (48.0, 36.0), 3
+    pos, vel = _field(seed, 2500, dims, 0.6)
+    pos[:300] = np.float32(7.5) + np.random.default_rng(seed).uniform(-1, 1, (300, 2)).astype(np.float32)
+    _run_both(W, O, dims, cs, pos, vel, 0, [1, 2, 7, 40])
+
+
+def test_reference_mode_cell_size_one(W, O):
+    dims = (200.0, 120.0)
+    pos, vel = _field(4, 9000, dims, 1.0)
+    _run_both(W, O, dims, 1, pos, vel, 0, [1, 5, 30])
+
+
+@pytest.mark.parametrize("iterations", [0, 1, 2, 4])
+def test_extended_mode_bit_exact(W, O, iterations):
+    dims = (96.0, 64.0)
+    pos, vel = _field(5, 3000, dims, 1.0)
+    _run_both(W, O, dims, 1, pos, vel, 1, [1, 3, 25], iterations=iterations, gravity=0.1)
+
+
+def test_extended_mode_cell_size_two(W, O):
+    dims = (128.0, 96.0)
+    pos, vel = _field(6, 6000, dims, 0.8)
+    _run_both(W, O, dims, 2, pos, vel, 1, [1, 10], iterations=3, gravity=0.05)
+
+
+def test_general_resort_on_large_displacement(W, O):
+    # velocities far above the clamp: the first frame moves particles by many
+    # cells, which takes the general re-sort; later frames the windowed one
+    dims = (64.0, 64.0)
+    pos, vel = _field(7, 2000, dims, 15.0)
+    flags = _run_both(W, O, dims, 1, pos, vel, 0, [1, 2, 12])
+    assert flags & W.FLAG_GENERAL_SORT
+
+
+def test_small_config_100_steps_bit_exact(W, O):
+    # 16,384 particles, 512x512, N(0, 2) velocities, cell 1, gravity 0.1,
+    # 4 iterations, 100 steps; bit-exact, so the kinetic energy, momentum and
+    # density histogram agree exactly too
+    from wrach_gb300 import workloads
+    dims, pos, vel = workloads.small()
+    sim = make_sim(W, dims, 1, 1, 4, 0.1)
+    try:
+        w = O.world(*dims, 1)
+        sim.add_particles(pos, vel)
+        sim.step(100)
+        gp, gv, gt = sim.read_frame()
+        rt, rp, rv, _ = O.step(w, O.extended_physics(4, 0.1), *O.pack(w, pos, vel, sim.capacity()), 100)
+        assert_frame_equal((gp, gv, gt), (rt, rp, rv), "100 steps")
+        ke_g, mom_g, h_g = frame_stats(gp, gv, dims)
+        ke_r, mom_r, h_r = frame_stats(rp, rv, dims)
+        assert abs(ke_g - ke_r) <= 0.01 * abs(ke_r)
+        assert np.allclose(mom_g, mom_r, rtol=0.01, atol=1e-3)
+        assert np.array_equal(h_g, h_r)
+    finally:
+        sim.close()
+
+
+def test_determinism(W):
+    dims = (300.0, 200.0)
+    pos, vel = _field(8, 20000, dims, 1.0)
+    out = []
+    for _ in range(2):
+        sim = make_sim(W, dims, 1, 1, 4, 0.1)
+        sim.add_particles(pos, vel)
+        sim.step(37)
+        out.append(sim.read_frame())
+        sim.close()
+    assert np.array_equal(out[0][2], out[1][2])
+    assert same_bits(out[0][0], out[1][0]) and same_bits(out[0][1], out[1][1])
+
+
+def test_capacity_error_keeps_state(W):
+    sim = make_sim(W, (20.0, 20.0), 1, capacity=100)
+    try:
+        pos, vel = _field(9, 80, (20.0, 20.0), 0.5)
+        sim.add_particles(pos, vel)
+        before = sim.read_frame()
+        with pytest.raises(W.CapacityError):
+            sim.add_particles(*_field(10, 30, (20.0, 20.0), 0.5))
+        after = sim.read_frame()
+        assert np.array_equal(before[2], after[2]) and same_bits(before[0], after[0])
+    finally:
+        sim.close()
+
+
+def test_empty_world_steps(W):
+    sim = make_sim(W, (50.0, 30.0), 1, 1)
+    try:
+        sim.step(5)
+        p, v, t = sim.read_frame()
+        assert len(p) == 0 and not t.any()
+        assert sim.flags() == 0
+    finally:
+        sim.close()
+
+
+def test_batched_worlds_match_single_world_oracle(W, O):
+    rng = np.random.default_rng(11)
+    dims = [(37.0, 23.0), (64.0, 64.0), (5.0, 90.0), (128.0, 17.0), (1.0, 1.0)]
+    counts = [300, 1500, 200, 900, 3]
+    cfg = W.WrachConfig(cell_size=1, mode=1, iterations=4, gravity=0.1, capacity=2000)
+    sim = W.Simulation(cfg, worlds=dims)
+    try:
+        refs = []
+        for k, (d, n) in enumerate(zip(dims, counts)):
+            pos = rng.uniform((0, 0), d, size=(n, 2)).astype(np.float32)
+            vel = rng.normal(0, 1.0, size=(n, 2)).astype(np.float32)
+            sim.add_particles(pos, vel, world=k)
+            w = O.world(d[0], d[1], 1)
+            refs.append((w, O.pack(w, pos, vel, 2000)))
+        for k, (w, ref) in enumerate(refs):
+            assert_frame_equal(sim.read_frame(k), ref, "world %d upload" % k)
+        sim.step(9)
+        ph = O.extended_physics(4, 0.1)
+        for k, (w, ref) in enumerate(refs):
+            want = O.step(w, ph, ref[0], ref[1], ref[2], 9)[:3]
+            assert_frame_equal(sim.read_frame(k), want, "world %d after 9 steps" % k)
+    finally:
+        sim.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_full_size_lattice_steps(W, O, mode):
+    # 1,000,000 particles, 1920x1080, cell 1: the benchmark workload
+    from wrach_gb300 import workloads
+    dims, pos, vel = workloads.lattice()
+    _run_both(W, O, dims, 1, pos, vel, mode, [1, 2, 10], iterations=4,
+              gravity=0.1 if mode else 0.0)
+
+
+def test_clustered_blobs_checked_every_100_steps(W, O):
+    # 4,000,000 particles in 32 blobs falling into a 4096x2048 basin, 2000
+    # steps; every 100 steps the GPU's own state is stepped once by the oracle
+    # and the next GPU frame (table, order, positions, velocities) must match
+    from wrach_gb300 import workloads
+    dims, pos, vel = workloads.blobs()
+    sim = make_sim(W, dims, 1, 1, 4, 0.1)
+    try:
+        w = O.world(*dims, 1)
+        ph = O.extended_physics(4, 0.1)
+        sim.add_particles(pos, vel)
+        done = 0
+        while done < 2000:
+            sim.step(99)
+            gp, gv, gt = sim.read_frame()
+            want = O.step(w, ph, gt, gp, gv, 1)[:3]
+            sim.step(1)
+            done += 100
+            assert_frame_equal(sim.read_frame(), want, "step %d" % done)
+            assert int(gt[-1]) == len(pos)
+    finally:
+        sim.close()

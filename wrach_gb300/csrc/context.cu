@@ -1,0 +1,778 @@
+// The C ABI (include/wrach.h): context lifetime, uploads, the frame loop and
+// readback.  Host orchestration of the kernels in solve.cu and rebin.cu.
+//
+// Device layout of a context (all worlds concatenated; world w owns the
+// global cells [cell_off_w, cell_off_w + gx_w * gy_w) and, in the frame, the
+// particles [cell_start[cell_off_w], cell_start[cell_off_w + cells_w])):
+//   pos, vel          binned state, float2 x capacity        (cell order)
+//   pos_o, vel_o      solve output, float2 x capacity        (same order)
+//   q1, q2            extended-mode Jacobi iterates
+//   cell_of[2]        cell of each binned particle (u32)
+//   cs[2]             cell-start table, cells + 1 u32 (ping-pong per frame)
+//   keys              next cell of each solve output (u32)
+//   kA kB iA iB hist  general re-sort scratch
+//   status            look-back words, one per tile of kTileCells cells
+//   ctrl              counters and sticky flags
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/wrach.h"
+#include "wrach_kernels.h"
+
+using wrach::Ctrl;
+using wrach::PhysDev;
+using wrach::WorldDev;
+
+namespace {
+
+struct Store {
+  float2* pos = nullptr;
+  float2* vel = nullptr;
+  uint32_t n = 0;
+  uint32_t cap = 0;
+};
+
+// Rust's saturating `f32 as i32` (NaN -> 0).
+int32_t sat_i32(float f) {
+  if (f != f) return 0;
+  if (f >= 2147483648.0f) return INT32_MAX;
+  if (f <= -2147483648.0f) return INT32_MIN;
+  return (int32_t)f;
+}
+
+// SpatialBin::get_cell_coord (runners/bevy/src/spatial_bin.rs:48-64).
+int32_t cell_coord(float x, uint32_t cs) {
+  volatile float d = (float)cs;  // keep the binary32 division
+  float q = std::trunc(x / d);
+  if (std::fmod(x, (float)d) < 0.0f) q = q - 1.0f;
+  return sat_i32(q);
+}
+
+__global__ void k_gather_u32(const uint32_t* __restrict__ src,
+                             const uint32_t* __restrict__ idx, uint32_t n,
+                             uint32_t* __restrict__ out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = src[idx[i]];
+}
+
+uint32_t bits_for(uint32_t v) {
+  uint32_t b = 0;
+  while (b < 32 && (v >> b) != 0) ++b;
+  return b;
+}
+
+}  // namespace
+
+struct WrachContext {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  WrachConfig cfg{};
+  PhysDev ph{};
+  uint32_t nworlds = 0;
+  std::vector<WorldDev> worlds_h;
+  std::vector<uint32_t> cap_h;   // frame capacity per world
+  std::vector<uint32_t> n_h;     // frame particles per world
+  std::vector<uint32_t> poff_h;  // first frame particle of each world
+  uint32_t ncells = 0;
+  uint32_t total_cap = 0;
+  uint32_t n = 0;
+  uint32_t max_world_cells = 0;
+  WorldDev* worlds_d = nullptr;
+  float2 *pos = nullptr, *vel = nullptr, *pos_o = nullptr, *vel_o = nullptr;
+  float2 *q1 = nullptr, *q2 = nullptr;
+  uint32_t* cell_of[2] = {nullptr, nullptr};
+  uint32_t* cs[2] = {nullptr, nullptr};
+  int cur = 0;
+  uint32_t* keys = nullptr;
+  uint32_t *kA = nullptr, *kB = nullptr, *iA = nullptr, *iB = nullptr;
+  size_t sort_cap = 0;
+  uint32_t* hist = nullptr;
+  uint64_t* status = nullptr;
+  uint32_t ntiles = 0;
+  Ctrl* ctrl = nullptr;
+  int rebin_grid = 0;
+  std::vector<Store> stores;
+  float2 *stage_pos = nullptr, *stage_vel = nullptr;
+  size_t stage_cap = 0;
+  uint32_t* table_tmp = nullptr;  // one world's reference-layout table
+  uint32_t* gather_idx = nullptr; // nworlds + 1
+  uint32_t* gather_out = nullptr;
+  std::string err;
+  uint64_t launches = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  bool graph_ok = true;
+  cudaEvent_t* event_hook = nullptr;  // wrach_profile_frame: one event per launch boundary
+  uint32_t event_count = 0;
+};
+
+namespace {
+
+int fail(WrachContext* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                             \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation                       \
+                           ? WRACH_ERR_OUT_OF_MEMORY                         \
+                           : WRACH_ERR_CUDA,                                 \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+void drop_graphs(WrachContext* ctx) {
+  for (auto& g : ctx->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+void release(WrachContext* ctx) {
+  drop_graphs(ctx);
+  void* ptrs[] = {ctx->worlds_d, ctx->pos, ctx->vel, ctx->pos_o, ctx->vel_o,
+                  ctx->q1, ctx->q2, ctx->cell_of[0], ctx->cell_of[1],
+                  ctx->cs[0], ctx->cs[1], ctx->keys, ctx->kA, ctx->kB,
+                  ctx->iA, ctx->iB, ctx->hist, ctx->status, ctx->ctrl,
+                  ctx->stage_pos, ctx->stage_vel, ctx->table_tmp,
+                  ctx->gather_idx, ctx->gather_out};
+  for (void* p : ptrs) dfree(p);
+  for (auto& s : ctx->stores) {
+    dfree(s.pos);
+    dfree(s.vel);
+  }
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int now = -1;
+    if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev)
+      cudaSetDevice(prev);
+  }
+};
+
+int ensure_sort_capacity(WrachContext* ctx, size_t need) {
+  if (need <= ctx->sort_cap) return WRACH_OK;
+  size_t cap = std::max(need, ctx->sort_cap * 2);
+  uint32_t** bufs[] = {&ctx->keys, &ctx->kA, &ctx->kB, &ctx->iA, &ctx->iB};
+  for (auto b : bufs) {
+    dfree(*b);
+    *b = nullptr;
+  }
+  for (auto b : bufs) CK(dalloc(b, cap));
+  ctx->sort_cap = cap;
+  drop_graphs(ctx);
+  return WRACH_OK;
+}
+
+int ensure_stage(WrachContext* ctx, size_t need) {
+  if (need <= ctx->stage_cap) return WRACH_OK;
+  size_t cap = std::max(need, ctx->stage_cap * 2);
+  dfree(ctx->stage_pos);
+  dfree(ctx->stage_vel);
+  ctx->stage_pos = ctx->stage_vel = nullptr;
+  CK(dalloc(&ctx->stage_pos, cap));
+  CK(dalloc(&ctx->stage_vel, cap));
+  ctx->stage_cap = cap;
+  return WRACH_OK;
+}
+
+int ensure_store(WrachContext* ctx, Store& s, size_t need) {
+  if (need <= s.cap) return WRACH_OK;
+  size_t cap = std::max<size_t>(need, (size_t)s.cap * 2);
+  if (cap > 0xFFFFFFF0ull) return fail(ctx, WRACH_ERR_CAPACITY, "store too large");
+  float2 *np = nullptr, *nv = nullptr;
+  CK(dalloc(&np, cap));
+  CK(dalloc(&nv, cap));
+  if (s.n) {
+    CK(cudaMemcpyAsync(np, s.pos, s.n * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(nv, s.vel, s.n * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  dfree(s.pos);
+  dfree(s.vel);
+  s.pos = np;
+  s.vel = nv;
+  s.cap = (uint32_t)cap;
+  return WRACH_OK;
+}
+
+wrach::SolveArgs solve_args(WrachContext* ctx) {
+  wrach::SolveArgs a{};
+  a.worlds = ctx->worlds_d;
+  a.nworlds = (int)ctx->nworlds;
+  a.ph = ctx->ph;
+  a.ncells = ctx->ncells;
+  a.n = ctx->n;
+  a.cell_start = ctx->cs[ctx->cur];
+  a.cell_of = ctx->cell_of[ctx->cur];
+  a.pos = ctx->pos;
+  a.vel = ctx->vel;
+  a.pos_out = ctx->pos_o;
+  a.vel_out = ctx->vel_o;
+  a.keys = ctx->keys;
+  a.ctrl = ctx->ctrl;
+  return a;
+}
+
+wrach::RebinArgs rebin_args(WrachContext* ctx) {
+  wrach::RebinArgs r{};
+  r.worlds = ctx->worlds_d;
+  r.nworlds = (int)ctx->nworlds;
+  r.ncells = ctx->ncells;
+  r.status = ctx->status;
+  r.ntiles = ctx->ntiles;
+  r.kA = ctx->kA;
+  r.kB = ctx->kB;
+  r.iA = ctx->iA;
+  r.iB = ctx->iB;
+  r.hist = ctx->hist;
+  r.key_bits = bits_for(ctx->ncells);
+  r.keys = ctx->keys;
+  r.ctrl = ctx->ctrl;
+  return r;
+}
+
+void mark(WrachContext* ctx) {
+  if (ctx->event_hook) cudaEventRecord(ctx->event_hook[ctx->event_count++], ctx->stream);
+}
+
+// One frame: solve (1 or `iterations` launches) then the rebin launch.
+int enqueue_frame(WrachContext* ctx) {
+  wrach::SolveArgs a = solve_args(ctx);
+  cudaStream_t st = ctx->stream;
+  mark(ctx);
+  if (ctx->ph.mode == WRACH_MODE_REFERENCE) {
+    CK(wrach::launch_solve_reference(a, st));
+    mark(ctx);
+    ctx->launches += 1;
+  } else {
+    const uint32_t K = ctx->ph.iterations;
+    if (K == 0) {
+      CK(wrach::launch_solve_extended(a, ctx->pos, ctx->pos_o, true, 0, st));
+      mark(ctx);
+      ctx->launches += 1;
+    } else {
+      const float2* src = ctx->pos;
+      for (uint32_t it = 0; it + 1 < K; ++it) {
+        float2* dst = (it & 1) ? ctx->q2 : ctx->q1;
+        CK(wrach::launch_solve_extended(a, src, dst, false, 1, st));
+        mark(ctx);
+        src = dst;
+      }
+      CK(wrach::launch_solve_extended(a, src, ctx->pos_o, true, 1, st));
+      mark(ctx);
+      ctx->launches += K;
+    }
+  }
+  wrach::RebinArgs r = rebin_args(ctx);
+  r.n = ctx->n;
+  r.dst_capacity = ctx->total_cap;
+  r.cs_old = ctx->cs[ctx->cur];
+  r.pos_src = ctx->pos_o;
+  r.vel_src = ctx->vel_o;
+  r.cs_new = ctx->cs[ctx->cur ^ 1];
+  r.pos_dst = ctx->pos;
+  r.vel_dst = ctx->vel;
+  r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
+  r.force_general = 0;
+  CK(wrach::launch_rebin(r, ctx->rebin_grid, st));
+  mark(ctx);
+  ctx->launches += 1;
+  ctx->cur ^= 1;
+  return WRACH_OK;
+}
+
+uint32_t frame_launches(const WrachContext* ctx) {
+  if (ctx->ph.mode == WRACH_MODE_REFERENCE) return 2;
+  return std::max<uint32_t>(ctx->ph.iterations, 1) + 1;
+}
+
+// One frame captured as a CUDA graph, instantiated once per table parity
+// (the frame reads cs[parity] and writes cs[parity ^ 1]).
+int build_graph(WrachContext* ctx) {
+  const int parity = ctx->cur;
+  const uint64_t launches = ctx->launches;
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->graph_ok = false;
+    return WRACH_OK;
+  }
+  int rc = enqueue_frame(ctx);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->cur = parity;
+  ctx->launches = launches;
+  if (rc != WRACH_OK || e != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    ctx->graph_ok = false;
+    ctx->err.clear();
+    return WRACH_OK;
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ctx->graph_ok = false;
+    return WRACH_OK;
+  }
+  ctx->graph[parity] = exec;
+  return WRACH_OK;
+}
+
+int world_settings_init(WorldDev& w, float width, float height, float ax,
+                        float ay, uint32_t cs) {
+  std::memset(&w, 0, sizeof(w));
+  w.dim_x = width;
+  w.dim_y = height;
+  w.ax = ax;
+  w.ay = ay;
+  w.cs = cs;
+  volatile float x1 = ax + width, y1 = ay + height;
+  w.x1 = x1;
+  w.y1 = y1;
+  const int32_t blx = cell_coord(ax, cs), bly = cell_coord(ay, cs);
+  const int32_t trx = cell_coord(x1, cs), try_ = cell_coord(y1, cs);
+  if (trx < blx || try_ < bly) return 1;
+  const int64_t gx = (int64_t)trx - blx + 1, gy = (int64_t)try_ - bly + 1;
+  if (gx * gy > 0x7FFFFFFFll) return 1;
+  w.gx = (uint32_t)gx;
+  w.gy = (uint32_t)gy;
+  w.blx = blx;
+  w.bly = bly;
+  return 0;
+}
+
+int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
+                WrachContext** out) {
+  if (!config || !out || nworlds == 0) return WRACH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  WrachContext* ctx = new (std::nothrow) WrachContext();
+  if (!ctx) return WRACH_ERR_OUT_OF_MEMORY;
+  ctx->cfg = *config;
+  const WrachConfig& c = ctx->cfg;
+  auto bad = [&](const char* m) {
+    int rc = fail(ctx, WRACH_ERR_INVALID_ARGUMENT, m);
+    delete ctx;
+    return rc;
+  };
+  if (c.cell_size == 0) return bad("cell_size must be positive");
+  if (c.mode != WRACH_MODE_REFERENCE && c.mode != WRACH_MODE_EXTENDED) return bad("unknown mode");
+  if (c.mode == WRACH_MODE_REFERENCE &&
+      (c.cell_capacity == 0 || c.cell_capacity > wrach::kMaxCellCapacity))
+    return bad("cell_capacity must be in 1..16");
+  if (!(c.min_distance > 0.0f) || !(c.max_velocity >= 0.0f)) return bad("bad physics constants");
+  if (c.iterations > 64) return bad("iterations must be at most 64");
+
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    int rc = fail(ctx, WRACH_ERR_UNSUPPORTED, "no CUDA device");
+    delete ctx;
+    return rc;
+  }
+  if (c.device < 0 || c.device >= ndev) return bad("device ordinal out of range");
+  ctx->device = c.device;
+  DeviceGuard guard(ctx->device);
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, ctx->device) != cudaSuccess ||
+      !(prop.major == 10 && prop.minor == 3)) {
+    int rc = fail(ctx, WRACH_ERR_UNSUPPORTED,
+                  std::string("this build targets sm_103a; device is ") + prop.name);
+    delete ctx;
+    return rc;
+  }
+
+  ctx->ph.mode = c.mode;
+  ctx->ph.iterations = c.mode == WRACH_MODE_REFERENCE ? 1u : c.iterations;
+  ctx->ph.gravity = c.mode == WRACH_MODE_REFERENCE ? 0.0f : c.gravity;
+  ctx->ph.min_d = c.min_distance;
+  ctx->ph.vmax = c.max_velocity;
+  ctx->ph.cap = c.cell_capacity;
+
+  ctx->nworlds = nworlds;
+  ctx->worlds_h.resize(nworlds);
+  ctx->cap_h.resize(nworlds);
+  ctx->n_h.assign(nworlds, 0);
+  ctx->poff_h.assign(nworlds, 0);
+  ctx->stores.resize(nworlds);
+  uint64_t cells = 0, cap = 0;
+  for (uint32_t w = 0; w < nworlds; ++w) {
+    const float wd = dims ? dims[2 * w] : c.width;
+    const float ht = dims ? dims[2 * w + 1] : c.height;
+    if (!(wd >= 0.0f) || !(ht >= 0.0f)) return bad("world dimensions must be non-negative");
+    if (world_settings_init(ctx->worlds_h[w], wd, ht, c.anchor_x, c.anchor_y, c.cell_size))
+      return bad("grid too large");
+    WorldDev& wd_ = ctx->worlds_h[w];
+    wd_.cell_off = (uint32_t)cells;
+    const uint64_t wc = (uint64_t)wd_.gx * wd_.gy;
+    cells += wc;
+    ctx->max_world_cells = std::max<uint32_t>(ctx->max_world_cells, (uint32_t)wc);
+    const uint32_t wcap = c.capacity ? c.capacity
+                                     : wrach_max_particles_per_frame((uint32_t)wc, c.cell_size);
+    ctx->cap_h[w] = wcap;
+    cap += wcap;
+    if (cells > 0xF0000000ull || cap > 0x7FFFFFFFull) return bad("grid or capacity too large");
+  }
+  ctx->ncells = (uint32_t)cells;
+  ctx->total_cap = (uint32_t)cap;
+  ctx->ntiles = (ctx->ncells + wrach::kTileCells - 1) / wrach::kTileCells;
+  ctx->rebin_grid = wrach::rebin_grid_size(ctx->device);
+  if (ctx->rebin_grid <= 0) {
+    int rc = fail(ctx, WRACH_ERR_CUDA, "cannot size the rebin grid (kernel image not loadable?)");
+    delete ctx;
+    return rc;
+  }
+
+  auto oom = [&](cudaError_t e) {
+    int rc = fail(ctx, e == cudaErrorMemoryAllocation ? WRACH_ERR_OUT_OF_MEMORY : WRACH_ERR_CUDA,
+                  std::string("allocation: ") + cudaGetErrorString(e));
+    cudaGetLastError();
+    release(ctx);
+    delete ctx;
+    return rc;
+  };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) return oom(e);
+  const size_t tc = ctx->total_cap;
+  if ((e = dalloc(&ctx->worlds_d, nworlds)) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->pos, tc)) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->vel, tc)) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->pos_o, tc)) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->vel_o, tc)) != cudaSuccess) return oom(e);
+  if (c.mode == WRACH_MODE_EXTENDED && ctx->ph.iterations >= 2) {
+    if ((e = dalloc(&ctx->q1, tc)) != cudaSuccess) return oom(e);
+    if ((e = dalloc(&ctx->q2, tc)) != cudaSuccess) return oom(e);
+  }
+  for (int i = 0; i < 2; ++i) {
+    if ((e = dalloc(&ctx->cell_of[i], tc)) != cudaSuccess) return oom(e);
+    if ((e = dalloc(&ctx->cs[i], (size_t)ctx->ncells + 1)) != cudaSuccess) return oom(e);
+    if ((e = cudaMemset(ctx->cs[i], 0, ((size_t)ctx->ncells + 1) * 4)) != cudaSuccess) return oom(e);
+  }
+  if ((e = dalloc(&ctx->hist, (size_t)256 * ctx->rebin_grid)) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->status, std::max<uint32_t>(ctx->ntiles, 1))) != cudaSuccess) return oom(e);
+  if ((e = cudaMemset(ctx->status, 0, sizeof(uint64_t) * std::max<uint32_t>(ctx->ntiles, 1))) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->ctrl, 1)) != cudaSuccess) return oom(e);
+  if ((e = cudaMemset(ctx->ctrl, 0, sizeof(Ctrl))) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->table_tmp, (size_t)ctx->max_world_cells + 2)) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->gather_idx, nworlds + 1)) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->gather_out, nworlds + 1)) != cudaSuccess) return oom(e);
+  {
+    std::vector<uint32_t> idx(nworlds + 1);
+    for (uint32_t w = 0; w < nworlds; ++w) idx[w] = ctx->worlds_h[w].cell_off;
+    idx[nworlds] = ctx->ncells;
+    if ((e = cudaMemcpy(ctx->gather_idx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return oom(e);
+  }
+  if ((e = cudaMemcpy(ctx->worlds_d, ctx->worlds_h.data(), nworlds * sizeof(WorldDev),
+                      cudaMemcpyHostToDevice)) != cudaSuccess)
+    return oom(e);
+  if (ensure_sort_capacity(ctx, tc) != WRACH_OK) {
+    int rc = WRACH_ERR_OUT_OF_MEMORY;
+    release(ctx);
+    delete ctx;
+    return rc;
+  }
+  *out = ctx;
+  return WRACH_OK;
+}
+
+int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
+                const float* vel, uint32_t n_add, cudaMemcpyKind kind,
+                bool replace) {
+  if (!ctx) return WRACH_ERR_INVALID_ARGUMENT;
+  if (world >= ctx->nworlds) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "world out of range");
+  if (n_add && (!pos || !vel)) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "null particle arrays");
+  DeviceGuard guard(ctx->device);
+  Store& s = ctx->stores[world];
+  const uint32_t old_n = s.n;
+  if (replace) s.n = 0;
+  int rc = ensure_store(ctx, s, (size_t)s.n + n_add);
+  if (rc) return rc;
+  if (n_add) {
+    CK(cudaMemcpyAsync(s.pos + s.n, pos, (size_t)n_add * sizeof(float2), kind, ctx->stream));
+    CK(cudaMemcpyAsync(s.vel + s.n, vel, (size_t)n_add * sizeof(float2), kind, ctx->stream));
+  }
+  s.n += n_add;
+
+  const uint32_t n_keep = ctx->n, n_new = s.n;
+  const size_t nsrc = (size_t)n_keep + n_new;
+  if (nsrc > 0xFFFFFFF0ull) {
+    s.n = old_n;
+    return fail(ctx, WRACH_ERR_CAPACITY, "too many particles");
+  }
+  if ((rc = ensure_stage(ctx, nsrc))) return rc;
+  if ((rc = ensure_sort_capacity(ctx, nsrc))) return rc;
+  if (n_keep) {
+    CK(cudaMemcpyAsync(ctx->stage_pos, ctx->pos, n_keep * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->stage_vel, ctx->vel, n_keep * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  if (n_new) {
+    CK(cudaMemcpyAsync(ctx->stage_pos + n_keep, s.pos, n_new * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->stage_vel + n_keep, s.vel, n_new * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  CK(wrach::launch_upload_keys(ctx->worlds_d, (int)ctx->nworlds, ctx->ncells, world, n_keep,
+                               ctx->cell_of[ctx->cur], n_new, s.pos, ctx->keys, ctx->stream));
+  ctx->launches += nsrc ? 1 : 0;
+  wrach::RebinArgs r = rebin_args(ctx);
+  r.n = (uint32_t)nsrc;
+  r.dst_capacity = ctx->total_cap;
+  r.cs_old = ctx->cs[ctx->cur];
+  r.pos_src = ctx->stage_pos;
+  r.vel_src = ctx->stage_vel;
+  r.cs_new = ctx->cs[ctx->cur ^ 1];
+  r.pos_dst = ctx->pos_o;
+  r.vel_dst = ctx->vel_o;
+  r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
+  r.force_general = 1;
+  CK(wrach::launch_rebin(r, ctx->rebin_grid, ctx->stream));
+  ctx->launches += 1;
+
+  // per-world counts from the new table
+  const uint32_t nw = ctx->nworlds;
+  k_gather_u32<<<(nw + 1 + 255) / 256, 256, 0, ctx->stream>>>(ctx->cs[ctx->cur ^ 1], ctx->gather_idx,
+                                                               nw + 1, ctx->gather_out);
+  CK(cudaGetLastError());
+  ctx->launches += 1;
+  std::vector<uint32_t> starts(nw + 1);
+  CK(cudaMemcpyAsync(starts.data(), ctx->gather_out, (nw + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (uint32_t w = 0; w < nw; ++w) {
+    const uint32_t cnt = starts[w + 1] - starts[w];
+    if (cnt > ctx->cap_h[w]) {
+      s.n = old_n;
+      return fail(ctx, WRACH_ERR_CAPACITY,
+                  "world " + std::to_string(w) + ": " + std::to_string(cnt) +
+                      " particles in the frame exceed its capacity " + std::to_string(ctx->cap_h[w]));
+    }
+  }
+  const uint32_t total = starts[nw];
+  if (total) {
+    CK(cudaMemcpyAsync(ctx->pos, ctx->pos_o, (size_t)total * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->vel, ctx->vel_o, (size_t)total * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  ctx->cur ^= 1;
+  ctx->n = total;
+  for (uint32_t w = 0; w < nw; ++w) {
+    ctx->n_h[w] = starts[w + 1] - starts[w];
+    ctx->poff_h[w] = starts[w];
+  }
+  drop_graphs(ctx);
+  ctx->graph_ok = true;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return WRACH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wrach_config_default(WrachConfig* c) {
+  if (!c) return WRACH_ERR_INVALID_ARGUMENT;
+  std::memset(c, 0, sizeof(*c));
+  c->width = 480.0f;
+  c->height = 352.0f;
+  c->cell_size = 3;
+  c->mode = WRACH_MODE_REFERENCE;
+  c->iterations = 4;
+  c->gravity = 0.0f;
+  c->min_distance = 1.0f;
+  c->max_velocity = 1.0f;
+  c->cell_capacity = 9;
+  c->capacity = 0;
+  c->device = 0;
+  return WRACH_OK;
+}
+
+uint32_t wrach_max_particles_per_frame(uint32_t cells, uint32_t cell_size) {
+  const uint32_t cs2 = (uint32_t)(uint16_t)(cell_size * cell_size);
+  const uint32_t normal = cells * cs2;
+  const uint32_t one_percent = (normal + 99u) / 100u;
+  return normal + 10u * one_percent;
+}
+
+int wrach_create(const WrachConfig* config, WrachContext** out) {
+  return create_impl(config, 1, nullptr, out);
+}
+
+int wrach_create_batch(const WrachConfig* config, uint32_t nworlds, const float* dims,
+                       WrachContext** out) {
+  if (!dims) return WRACH_ERR_INVALID_ARGUMENT;
+  return create_impl(config, nworlds, dims, out);
+}
+
+int wrach_destroy(WrachContext* ctx) {
+  if (!ctx) return WRACH_ERR_INVALID_ARGUMENT;
+  {
+    DeviceGuard guard(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    release(ctx);
+  }
+  delete ctx;
+  return WRACH_OK;
+}
+
+int wrach_add_particles(WrachContext* ctx, uint32_t world, const float* pos, const float* vel,
+                        uint32_t n) {
+  return upload_impl(ctx, world, pos, vel, n, cudaMemcpyHostToDevice, false);
+}
+
+int wrach_set_particles(WrachContext* ctx, uint32_t world, const float* pos, const float* vel,
+                        uint32_t n) {
+  return upload_impl(ctx, world, pos, vel, n, cudaMemcpyHostToDevice, true);
+}
+
+int wrach_add_particles_device(WrachContext* ctx, uint32_t world, const float* d_pos,
+                               const float* d_vel, uint32_t n) {
+  return upload_impl(ctx, world, d_pos, d_vel, n, cudaMemcpyDeviceToDevice, false);
+}
+
+int wrach_step(WrachContext* ctx, uint32_t nsteps) {
+  if (!ctx) return WRACH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(ctx->device);
+  for (uint32_t s = 0; s < nsteps; ++s) {
+    if (ctx->graph_ok && !ctx->graph[ctx->cur]) {
+      int rc = build_graph(ctx);
+      if (rc) return rc;
+    }
+    if (ctx->graph_ok && ctx->graph[ctx->cur]) {
+      CK(cudaGraphLaunch(ctx->graph[ctx->cur], ctx->stream));
+      ctx->launches += frame_launches(ctx);
+      ctx->cur ^= 1;
+    } else {
+      int rc = enqueue_frame(ctx);
+      if (rc) return rc;
+    }
+  }
+  return WRACH_OK;
+}
+
+int wrach_profile_frame(WrachContext* ctx, float* ms, uint32_t cap, uint32_t* count) {
+  if (!ctx || !count) return WRACH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(ctx->device);
+  const uint32_t nl = frame_launches(ctx);
+  *count = nl;
+  if (!ms || cap < nl) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "profile buffer too small");
+  std::vector<cudaEvent_t> ev(nl + 1);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  ctx->event_hook = ev.data();
+  ctx->event_count = 0;
+  int rc = enqueue_frame(ctx);
+  ctx->event_hook = nullptr;
+  if (rc == WRACH_OK) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (uint32_t i = 0; i < nl; ++i) CK(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
+int wrach_read(WrachContext* ctx, uint32_t world, float* positions, float* velocities,
+               uint32_t* indices, uint32_t capacity) {
+  if (!ctx) return WRACH_ERR_INVALID_ARGUMENT;
+  if (world >= ctx->nworlds) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "world out of range");
+  DeviceGuard guard(ctx->device);
+  const uint32_t n = ctx->n_h[world], off = ctx->poff_h[world];
+  if ((positions || velocities) && capacity < ctx->cap_h[world])
+    return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "capacity smaller than the world's frame capacity");
+  if (positions && n)
+    CK(cudaMemcpyAsync(positions, ctx->pos + off, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if (velocities && n)
+    CK(cudaMemcpyAsync(velocities, ctx->vel + off, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  const WorldDev& w = ctx->worlds_h[world];
+  const uint32_t cells = w.gx * w.gy;
+  if (indices) {
+    if (ctx->nworlds == 1) {
+      CK(cudaMemcpyAsync(indices + 1, ctx->cs[ctx->cur], ((size_t)cells + 1) * 4,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+    } else {
+      CK(wrach::launch_world_table(ctx->cs[ctx->cur], w.cell_off, cells, ctx->table_tmp, ctx->stream));
+      ctx->launches += 1;
+      CK(cudaMemcpyAsync(indices, ctx->table_tmp, ((size_t)cells + 2) * 4, cudaMemcpyDeviceToHost,
+                         ctx->stream));
+    }
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (indices && ctx->nworlds == 1) indices[0] = 0;
+  if (positions && capacity > n) std::memset(positions + 2 * (size_t)n, 0, (size_t)(capacity - n) * 8);
+  if (velocities && capacity > n) std::memset(velocities + 2 * (size_t)n, 0, (size_t)(capacity - n) * 8);
+  return WRACH_OK;
+}
+
+int wrach_tick(WrachContext* ctx, uint32_t world, float* positions, float* velocities,
+               uint32_t* indices, uint32_t capacity) {
+  int rc = wrach_step(ctx, 1);
+  if (rc) return rc;
+  return wrach_read(ctx, world, positions, velocities, indices, capacity);
+}
+
+int wrach_get_settings(WrachContext* ctx, uint32_t world, WrachWorldSettings* out) {
+  if (!ctx || !out || world >= ctx->nworlds) return WRACH_ERR_INVALID_ARGUMENT;
+  const WorldDev& w = ctx->worlds_h[world];
+  out->view_dimensions[0] = w.dim_x;
+  out->view_dimensions[1] = w.dim_y;
+  out->view_anchor[0] = w.ax;
+  out->view_anchor[1] = w.ay;
+  out->grid_dimensions[0] = w.gx;
+  out->grid_dimensions[1] = w.gy;
+  out->cell_size = w.cs;
+  out->particles_in_frame_count = ctx->n_h[world];
+  return WRACH_OK;
+}
+
+uint32_t wrach_capacity(WrachContext* ctx, uint32_t world) {
+  if (!ctx || world >= ctx->nworlds) return 0;
+  return ctx->cap_h[world];
+}
+
+uint32_t wrach_num_worlds(WrachContext* ctx) { return ctx ? ctx->nworlds : 0; }
+
+int wrach_sync(WrachContext* ctx) {
+  if (!ctx) return WRACH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(ctx->device);
+  CK(cudaStreamSynchronize(ctx->stream));
+  return WRACH_OK;
+}
+
+int wrach_flags(WrachContext* ctx, uint32_t* flags) {
+  if (!ctx || !flags) return WRACH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(ctx->device);
+  Ctrl h{};
+  CK(cudaMemcpyAsync(&h, ctx->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *flags = h.flags;
+  return WRACH_OK;
+}
+
+const char* wrach_last_error(WrachContext* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+uint64_t wrach_kernel_launches(WrachContext* ctx) { return ctx ? ctx->launches : 0; }
+
+void* wrach_stream(WrachContext* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+}  // extern "C"

@@ -1,0 +1,158 @@
+// Internal device-side types and helpers shared by the kernels of the wrach
+// GB300 library.  Every translation unit that includes this file is compiled
+// with -fmad=false and IEEE division/square root, so the arithmetic below is
+// binary32 round-to-nearest with no contraction: the contract under which the
+// reference's CPU known-answer test (shaders/physics/src/particles.rs:128-146)
+// reproduces bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace wrach {
+
+// One world as the kernels see it (48 bytes).  The first eight fields are the
+// reference's uniform (runners/bevy/src/config_shader.rs:15-29) minus the
+// particle count, which lives in the cell-start table.
+struct WorldDev {
+  float dim_x, dim_y;  // view_dimensions
+  float ax, ay;        // view_anchor
+  uint32_t gx, gy;     // grid_dimensions
+  uint32_t cs;         // cell_size
+  uint32_t cell_off;   // global index of the world's first cell
+  float x1, y1;        // anchor + dimensions, summed in binary32 as
+                       // Particle::enforce_boundaries does (particle.rs:47-52)
+  int32_t blx, bly;    // cell coordinate of the grid's bottom-left cell
+};
+
+struct PhysDev {
+  uint32_t mode;        // 0 reference, 1 extended
+  uint32_t iterations;  // extended only
+  float gravity;
+  float min_d;
+  float vmax;
+  uint32_t cap;         // reference cell capacity
+};
+
+// Device control block: counters for the persistent rebin kernel, the solve's
+// displacement bound and the sticky flags.  Zeroed at create; every launch of
+// the rebin kernel leaves ticket/exit_count/dmax at zero again.
+struct Ctrl {
+  uint32_t ticket;      // next windowed tile
+  uint32_t exit_count;  // rebin blocks finished in this launch
+  uint32_t epoch;       // rebin launch counter, tags the tile status words
+  uint32_t dmax;        // max cell displacement seen by the last solve
+  uint32_t flags;       // sticky WRACH_FLAG_* bits
+  uint32_t bar_count;   // grid barrier arrivals
+  uint32_t bar_gen;     // grid barrier generation
+  uint32_t general;     // frames that took the general re-sort
+  uint32_t overflow;    // particles dropped for lack of destination room
+  uint32_t pad[7];
+};
+
+constexpr uint32_t kFlagOutOfGrid = 1u;
+constexpr uint32_t kFlagNaN = 2u;
+constexpr uint32_t kFlagTimeout = 4u;
+constexpr uint32_t kFlagGeneralSort = 8u;
+
+// Largest per-frame cell displacement the windowed rebin handles; a frame
+// that moves any particle further is re-sorted by the general path.
+constexpr uint32_t kMaxWindow = 3;
+
+// Maximum reference-mode cell capacity held in registers/local memory.
+constexpr uint32_t kMaxCellCapacity = 16;
+
+// World of a global cell index: the last world whose cell_off <= c.
+__device__ __forceinline__ int world_of_cell(const WorldDev* __restrict__ W,
+                                             int nworlds, uint32_t c) {
+  int lo = 0, hi = nworlds - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&W[mid].cell_off) <= c)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// Frame-time cell of one axis (assets/shaders/particles_per_cell.wgsl:14-27):
+// floor((p - anchor) / cell_size).  Out-of-grid and NaN inputs, undefined in
+// the WGSL, are clamped into the grid (NaN -> 0) and flagged.
+__device__ __forceinline__ uint32_t axis_cell(float p, float a, uint32_t cs,
+                                              uint32_t g, uint32_t& flags) {
+  float f = floorf(__fdiv_rn(__fsub_rn(p, a), (float)cs));
+  if (!(f >= 0.0f)) {
+    flags |= (f != f) ? (kFlagNaN | kFlagOutOfGrid) : kFlagOutOfGrid;
+    return 0u;
+  }
+  if (f >= (float)g) {
+    flags |= kFlagOutOfGrid;
+    return g - 1u;
+  }
+  return (uint32_t)f;
+}
+
+// Particle::enforce_boundaries + enforce_velocity
+// (shaders/physics/src/particle.rs:46-77).  The clamp is Rust's f32::clamp:
+// compare-and-replace, NaN passes through.
+__device__ __forceinline__ void enforce_limits(const WorldDev& w, float vmax,
+                                               float& px, float& py, float& vx,
+                                               float& vy) {
+  if (px > w.x1) { px = w.x1; vx = -vx; }
+  if (px < w.ax) { px = w.ax; vx = -vx; }
+  if (py > w.y1) { py = w.y1; vy = -vy; }
+  if (py < w.ay) { py = w.ay; vy = -vy; }
+  if (vx < -vmax) vx = -vmax;
+  if (vx > vmax) vx = vmax;
+  if (vy < -vmax) vy = -vmax;
+  if (vy > vmax) vy = vmax;
+}
+
+// The reference's pair push factor (shaders/physics/src/particles.rs:62-93):
+// returns false when the pair is farther apart than min_d, otherwise the
+// force 0.5 * (min_d - d) / d with d == 0 replaced by 0.0001.
+__device__ __forceinline__ bool push_factor(float ex, float ey, float min_d,
+                                            float& f) {
+  float d = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
+  if (d > min_d) return false;
+  if (d == 0.0f) d = 0.0001f;
+  f = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(min_d, d)), d);
+  return true;
+}
+
+__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(uint64_t* p, uint64_t v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded device waits give up after this many nanoseconds and raise
+// kFlagTimeout instead of hanging the GPU.
+constexpr uint64_t kWaitLimitNs = 1000000000ull;
+
+// Warp-reduce helpers.
+__device__ __forceinline__ uint32_t warp_max_u32(uint32_t v) {
+  return __reduce_max_sync(0xffffffffu, v);
+}
+__device__ __forceinline__ uint32_t warp_or_u32(uint32_t v) {
+  return __reduce_or_sync(0xffffffffu, v);
+}
+
+}  // namespace wrach

@@ -1,0 +1,83 @@
+// Host-side declarations of the kernel launchers (internal to the library).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "wrach_internal.cuh"
+
+namespace wrach {
+
+struct SolveArgs {
+  const WorldDev* worlds;
+  int nworlds;
+  PhysDev ph;
+  uint32_t ncells;              // cells over all worlds
+  uint32_t n;                   // particles over all worlds
+  const uint32_t* cell_start;   // ncells + 1
+  const uint32_t* cell_of;      // n, cell of each binned particle
+  const float2* pos;            // binned state
+  const float2* vel;
+  float2* pos_out;              // solve output, same order
+  float2* vel_out;
+  uint32_t* keys;               // next cell of each output particle
+  Ctrl* ctrl;
+};
+
+cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st);
+cudaError_t launch_solve_extended(const SolveArgs& a, const float2* qin,
+                                  float2* qout, bool final_pass, int do_push,
+                                  cudaStream_t st);
+
+// Rebin: stable counting sort of `n` source particles by key into cell
+// order, writing a fresh cell-start table.  Persistent cooperative kernel.
+struct RebinArgs {
+  const WorldDev* worlds;
+  int nworlds;
+  uint32_t ncells;
+  uint32_t n;                   // source particles
+  uint32_t dst_capacity;        // room in pos_dst/vel_dst/cell_dst
+  const uint32_t* keys;         // n source keys, ncells = leave out
+  const uint32_t* cs_old;       // old table (windowed path)
+  const float2* pos_src;
+  const float2* vel_src;
+  uint32_t* cs_new;             // ncells + 1
+  float2* pos_dst;
+  float2* vel_dst;
+  uint32_t* cell_dst;
+  uint64_t* status;             // one word per tile
+  uint32_t ntiles;
+  uint32_t* kA;                 // general path scratch, n each
+  uint32_t* kB;
+  uint32_t* iA;
+  uint32_t* iB;
+  uint32_t* hist;               // 256 * grid
+  uint32_t key_bits;
+  int force_general;
+  Ctrl* ctrl;
+};
+
+constexpr uint32_t kRebinThreads = 256;
+constexpr uint32_t kCellsPerThread = 4;
+constexpr uint32_t kTileCells = kRebinThreads * kCellsPerThread;
+
+// Blocks the cooperative rebin kernel launches with on `device`.
+int rebin_grid_size(int device);
+cudaError_t launch_rebin(const RebinArgs& a, int grid, cudaStream_t st);
+
+// Keys for an upload re-pack: the first n_keep sources are particles of the
+// current frame (their cell, or `ncells` if they belong to world `target`),
+// the next n_new are store particles of world `target` binned as
+// SpatialBin::get_cell_coord does (ncells if outside the grid).
+cudaError_t launch_upload_keys(const WorldDev* worlds, int nworlds,
+                               uint32_t ncells, uint32_t target,
+                               uint32_t n_keep, const uint32_t* cell_of,
+                               uint32_t n_new, const float2* new_pos,
+                               uint32_t* keys, cudaStream_t st);
+
+// Reference-layout table of one world (cells + 2 entries) from the global
+// cell-start table.
+cudaError_t launch_world_table(const uint32_t* cell_start, uint32_t cell_off,
+                               uint32_t cells, uint32_t* out, cudaStream_t st);
+
+}  // namespace wrach
