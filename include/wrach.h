@@ -44,7 +44,6 @@ extern "C" {
 #define WRACH_FLAG_OUT_OF_GRID 1u /* a key was clamped into the grid */
 #define WRACH_FLAG_NAN 2u         /* a non-finite position was binned */
 #define WRACH_FLAG_TIMEOUT 4u     /* a bounded device wait gave up */
-#define WRACH_FLAG_GENERAL_SORT 8u /* a frame needed the general re-sort */
 
 /* The reference's 32-byte shader uniform, field for field
  * (runners/bevy/src/config_shader.rs:15-29, shaders/shared/src/lib.rs:19-31,
@@ -71,10 +70,12 @@ typedef struct WrachConfig {
   float gravity;           /* EXTENDED only, px/frame^2 (default 0) */
   float min_distance;      /* default 1.0 */
   float max_velocity;      /* default 1.0 */
-  uint32_t cell_capacity;  /* REFERENCE only, default 9 */
+  uint32_t cell_capacity;  /* particles of a cell that interact, 1..16,
+                              default 9 */
   uint32_t capacity;       /* 0 = max_particles_per_frame of the grid */
   int32_t device;          /* CUDA ordinal (default 0) */
-  uint32_t reserved[7];
+  uint32_t rebin_blocks;   /* blocks of the rebin kernel, 0 = all that fit */
+  uint32_t reserved[6];
 } WrachConfig;
 
 typedef struct WrachContext WrachContext;
@@ -151,6 +152,27 @@ int wrach_sync(WrachContext *ctx);
 
 /* Sticky device flags (WRACH_FLAG_*) seen since create; blocks. */
 int wrach_flags(WrachContext *ctx, uint32_t *flags);
+
+/* Counters of the device side (no counterpart in the reference). */
+typedef struct WrachStats {
+  uint32_t flags;             /* sticky WRACH_FLAG_* bits */
+  uint32_t frames;            /* frames stepped since create */
+  uint32_t overflow;          /* particles without destination room */
+  uint32_t rebin_blocks;      /* co-resident blocks of the rebin kernel */
+  uint32_t tiles;             /* tiles of the cell table */
+  uint32_t particles;         /* particles in the frame, all worlds */
+  uint32_t cells;             /* grid cells, all worlds */
+  uint32_t reserved[9];
+} WrachStats;
+
+/* Reads the counters; blocks. */
+int wrach_stats(WrachContext *ctx, WrachStats *out);
+
+/* Phase trace of the latest rebin launch: %globaltimer (ns) at each phase
+ * boundary, as recorded by its first block; *count receives the number of
+ * entries (at most 32).  Blocks.  No counterpart in the reference. */
+int wrach_rebin_trace(WrachContext *ctx, uint64_t *ns, uint32_t cap,
+                      uint32_t *count);
 
 /* The last error message of the context ("" if none). */
 const char *wrach_last_error(WrachContext *ctx);

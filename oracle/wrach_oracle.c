@@ -279,26 +279,31 @@ DEFINE_LIMITS(double, f64)
     }                                                                          \
   }
 
-/* Mode 1 (extended physics; not in the reference, parity unpinned by it):
+/* Mode 1 (extended physics; not in the reference, parity unpinned by it).
+ * The reference's per-cell physics widened to the 3x3 cell neighbourhood and
+ * iterated, with gravity.  As in the reference (cell.rs:29-30, 79-95) only
+ * the first `cell_capacity` particles of a cell (in table order) take part in
+ * the pair pushes; the rest of an over-full cell only integrate.
  *   q = p
- *   repeat `iterations` times (Jacobi, every particle reads the previous q):
- *     for particle i of cell (cx, cy):
+ *   repeat `iterations` times (Jacobi: every particle reads the previous q):
+ *     for each taking-part particle i of cell (cx, cy):
  *       acc = 0; for the 3x3 cells around (cx, cy) in row-major order, for
- *       each particle j != i in table order:
+ *       each taking-part particle j != i of that cell in table order:
  *         d = |q_i - q_j|; skip if d > min; if d == 0: d = 0.0001
  *         f = 0.5 * (min - d) / d          (the reference's pair push)
  *         acc += (q_j - q_i) * f
  *       q_i' = q_i - acc
  *   then v.y -= gravity; p = q + v; boundaries; velocity clamp.
- * With every pair's contribution to i and j exact negatives of each other the
- * push is momentum-conserving, and the fixed summation order makes it
- * deterministic under any parallel schedule. */
+ * Velocities change only at the walls and the clamp, as in the reference.
+ * Every pair's contributions to i and j are exact negatives, so the push is
+ * momentum-conserving; the fixed summation order makes it deterministic under
+ * any parallel schedule. */
 #define DEFINE_SOLVE_X(T, SUF, SQRT)                                           \
   static void solve_x_##SUF(const wo_world *w, const wo_physics *ph,           \
                             const uint32_t *table, const T *pin,               \
                             const T *vin, T *pout, T *vout) {                  \
     int64_t gx = w->grid_dimensions[0], gy = w->grid_dimensions[1];            \
-    uint32_t n = table[gx * gy + 1];                                           \
+    uint32_t n = table[gx * gy + 1], cap = ph->cell_capacity;                  \
     T mind = (T)ph->min_distance, vmax = (T)ph->max_velocity;                  \
     T *qa = (T *)malloc(sizeof(T) * 2 * (n ? n : 1));                          \
     T *qb = (T *)malloc(sizeof(T) * 2 * (n ? n : 1));                          \
@@ -308,26 +313,34 @@ DEFINE_LIMITS(double, f64)
       for (int64_t cy = 0; cy < gy; ++cy)                                      \
         for (int64_t cx = 0; cx < gx; ++cx) {                                  \
           uint32_t s = table[cy * gx + cx + 1], e = table[cy * gx + cx + 2];   \
-          int64_t x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < gx ? cx + 1 : gx - 1;\
-          for (uint32_t i = s; i < e; ++i) {                                   \
+          uint32_t m = e - s < cap ? e - s : cap;                              \
+          for (uint32_t i = s; i < s + m; ++i) {                               \
             T qx = qa[2 * i], qy = qa[2 * i + 1], ax = 0, ay = 0;              \
             for (int64_t ny = cy - 1; ny <= cy + 1; ++ny) {                    \
               if (ny < 0 || ny >= gy) continue;                                \
-              uint32_t js = table[ny * gx + x0 + 1];                           \
-              uint32_t je = table[ny * gx + x1 + 2];                           \
-              for (uint32_t j = js; j < je; ++j) {                             \
-                if (j == i) continue;                                          \
-                T dx = qa[2 * j] - qx, dy = qa[2 * j + 1] - qy;                \
-                T d = SQRT(dx * dx + dy * dy);                                 \
-                if (d > mind) continue;                                        \
-                if (d == (T)0) d = (T)0.0001f;                                 \
-                T f = ((T)0.5 * (mind - d)) / d;                               \
-                ax = ax + dx * f;                                              \
-                ay = ay + dy * f;                                              \
+              for (int64_t nx = cx - 1; nx <= cx + 1; ++nx) {                  \
+                if (nx < 0 || nx >= gx) continue;                              \
+                uint32_t js = table[ny * gx + nx + 1];                         \
+                uint32_t je = table[ny * gx + nx + 2];                         \
+                if (je - js > cap) je = js + cap;                              \
+                for (uint32_t j = js; j < je; ++j) {                           \
+                  if (j == i) continue;                                        \
+                  T dx = qa[2 * j] - qx, dy = qa[2 * j + 1] - qy;              \
+                  T d = SQRT(dx * dx + dy * dy);                               \
+                  if (d > mind) continue;                                      \
+                  if (d == (T)0) d = (T)0.0001f;                               \
+                  T f = ((T)0.5 * (mind - d)) / d;                             \
+                  ax = ax + dx * f;                                            \
+                  ay = ay + dy * f;                                            \
+                }                                                              \
               }                                                                \
             }                                                                  \
             qb[2 * i] = qx - ax;                                               \
             qb[2 * i + 1] = qy - ay;                                           \
+          }                                                                    \
+          for (uint32_t i = s + m; i < e; ++i) {                               \
+            qb[2 * i] = qa[2 * i];                                             \
+            qb[2 * i + 1] = qa[2 * i + 1];                                     \
           }                                                                    \
         }                                                                      \
       T *t = qa; qa = qb; qb = t;                                              \

@@ -67,3 +67,19 @@ def test_missing_library_fails_loudly(W, monkeypatch):
     monkeypatch.setattr(W._lib, "LIB_PATH", "/nonexistent/libwrach_gb300.so")
     with pytest.raises(ImportError):
         W._lib.load()
+
+
+def test_grid_width_division_constants():
+    # cell (x, y) = (c - y * gx, (c * m) >> s) with m = floor(2^(31+l)/gx) + 1,
+    # s = 31 + l, l = ceil(log2 gx): exact for every c < 2^31 (the kernels'
+    # cell indices stay below 2^31)
+    import random
+    rng = random.Random(0)
+    for gx in list(range(1, 3000)) + [1921, 4097, 65535, 65536, 1 << 20, 99991]:
+        l = 0
+        while (1 << l) < gx:
+            l += 1
+        m, s = (1 << (31 + l)) // gx + 1, 31 + l
+        assert m < 2 ** 32
+        for x in [0, 1, gx - 1, gx, gx + 1, 2 ** 31 - 1] + [rng.randrange(2 ** 31) for _ in range(50)]:
+            assert (x * m) >> s == x // gx

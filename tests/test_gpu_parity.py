@@ -90,7 +90,7 @@ def test_reference_mode_bit_exact(W, O, seed):
     dims, cs = (48.0, 36.0), 3
     pos, vel = _field(seed, 2500, dims, 0.6)
     pos[:300] = np.float32(7.5) + np.random.default_rng(seed).uniform(-1, 1, (300, 2)).astype(np.float32)
-    _run_both(W, O, dims, cs, pos, vel, 0, [1, 2, 7, 40])
+    _run_both(W, O, dims, cs, pos, vel, 0, [1, 2, 7, 40], capacity=4000)
 
 
 def test_reference_mode_cell_size_one(W, O):
@@ -112,13 +112,13 @@ def test_extended_mode_cell_size_two(W, O):
     _run_both(W, O, dims, 2, pos, vel, 1, [1, 10], iterations=3, gravity=0.05)
 
 
-def test_general_resort_on_large_displacement(W, O):
+def test_large_displacement_frame(W, O):
     # velocities far above the clamp: the first frame moves particles by many
-    # cells, which takes the general re-sort; later frames the windowed one
+    # cells at once
     dims = (64.0, 64.0)
     pos, vel = _field(7, 2000, dims, 15.0)
     flags = _run_both(W, O, dims, 1, pos, vel, 0, [1, 2, 12])
-    assert flags & W.FLAG_GENERAL_SORT
+    assert flags == 0
 
 
 def test_small_config_100_steps_bit_exact(W, O):
@@ -237,5 +237,44 @@ def test_clustered_blobs_checked_every_100_steps(W, O):
             done += 100
             assert_frame_equal(sim.read_frame(), want, "step %d" % done)
             assert int(gt[-1]) == len(pos)
+    finally:
+        sim.close()
+
+
+def test_few_fast_particles(W, O):
+    # a quiet field with a handful of fast particles that jump several cells
+    # in the first frame
+    dims = (120.0, 90.0)
+    pos, vel = _field(12, 5000, dims, 0.2)
+    fast = np.random.default_rng(13).choice(len(pos), 60, replace=False)
+    vel[fast] = np.random.default_rng(14).uniform(-6, 6, size=(60, 2)).astype(np.float32)
+    sim = make_sim(W, dims, 1, 0)
+    try:
+        sim.add_particles(pos, vel)
+        w = O.world(*dims, 1)
+        ref = O.pack(w, pos, vel, sim.capacity())
+        sim.step(1)
+        ref = O.step(w, O.reference_physics(), *ref, 1)[:3]
+        assert_frame_equal(sim.read_frame(), ref, "frame with fast particles")
+        assert sim.stats()["frames"] == 1
+        sim.step(5)
+        ref = O.step(w, O.reference_physics(), *ref, 5)[:3]
+        assert_frame_equal(sim.read_frame(), ref, "after 6 frames")
+    finally:
+        sim.close()
+
+
+def test_many_fast_particles(W, O):
+    dims = (200.0, 200.0)
+    pos, vel = _field(15, 8000, dims, 5.0)
+    sim = make_sim(W, dims, 1, 1, 2, 0.1)
+    try:
+        sim.add_particles(pos, vel)
+        w = O.world(*dims, 1)
+        ref = O.pack(w, pos, vel, sim.capacity())
+        sim.step(2)
+        ref = O.step(w, O.extended_physics(2, 0.1), *ref, 2)[:3]
+        assert_frame_equal(sim.read_frame(), ref, "fast frames")
+        assert sim.stats()["overflow"] == 0
     finally:
         sim.close()

@@ -3,7 +3,7 @@ for GB300 (sm_103a) behind a C ABI (include/wrach.h).
 
 `build()` compiles the library in-tree; `Simulation` and `WrachAPI` drive it.
 """
-from ._lib import (FLAG_GENERAL_SORT, FLAG_NAN, FLAG_OUT_OF_GRID, FLAG_TIMEOUT,
+from ._lib import (FLAG_NAN, FLAG_OUT_OF_GRID, FLAG_TIMEOUT,
                    MODE_EXTENDED, MODE_REFERENCE, CapacityError, WrachError)
 from .api import (PackedData, Particle, Simulation, Vec2, WrachAPI, WrachConfig,
                   WrachState)
@@ -12,5 +12,5 @@ from .build import build
 __all__ = [
     "build", "Simulation", "WrachAPI", "WrachConfig", "WrachState", "PackedData",
     "Particle", "Vec2", "WrachError", "CapacityError", "MODE_REFERENCE", "MODE_EXTENDED",
-    "FLAG_OUT_OF_GRID", "FLAG_NAN", "FLAG_TIMEOUT", "FLAG_GENERAL_SORT",
+    "FLAG_OUT_OF_GRID", "FLAG_NAN", "FLAG_TIMEOUT",
 ]

@@ -23,7 +23,6 @@ MODE_EXTENDED = 1
 FLAG_OUT_OF_GRID = 1
 FLAG_NAN = 2
 FLAG_TIMEOUT = 4
-FLAG_GENERAL_SORT = 8
 
 ERROR_NAMES = {
     1: "invalid argument", 2: "capacity exceeded", 3: "CUDA error",
@@ -64,7 +63,15 @@ class Config(ctypes.Structure):
                 ("cell_capacity", ctypes.c_uint32),
                 ("capacity", ctypes.c_uint32),
                 ("device", ctypes.c_int32),
-                ("reserved", ctypes.c_uint32 * 7)]
+                ("rebin_blocks", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 6)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("flags", ctypes.c_uint32), ("frames", ctypes.c_uint32),
+                ("overflow", ctypes.c_uint32), ("rebin_blocks", ctypes.c_uint32),
+                ("tiles", ctypes.c_uint32), ("particles", ctypes.c_uint32),
+                ("cells", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 9)]
 
 
 # name -> (restype, argtypes); every symbol include/wrach.h declares
@@ -90,6 +97,8 @@ SIGNATURES = {
     "wrach_num_worlds": (ctypes.c_uint32, [_P]),
     "wrach_sync": (ctypes.c_int, [_P]),
     "wrach_flags": (ctypes.c_int, [_P, _U]),
+    "wrach_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
+    "wrach_rebin_trace": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, _U]),
     "wrach_last_error": (ctypes.c_char_p, [_P]),
     "wrach_kernel_launches": (ctypes.c_uint64, [_P]),
     "wrach_stream": (ctypes.c_void_p, [_P]),

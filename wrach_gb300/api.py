@@ -49,6 +49,7 @@ class WrachConfig:
     capacity: int = 0
     anchor: Tuple[float, float] = (0.0, 0.0)
     device: int = 0
+    rebin_blocks: int = 0
 
     def to_c(self):
         c = _lib.Config()
@@ -64,6 +65,7 @@ class WrachConfig:
         c.cell_capacity = int(self.cell_capacity)
         c.capacity = int(self.capacity)
         c.device = int(self.device)
+        c.rebin_blocks = int(self.rebin_blocks)
         return c
 
 
@@ -191,6 +193,19 @@ class Simulation:
         f = ctypes.c_uint32(0)
         self._check(self._L.wrach_flags(self._ctx, ctypes.byref(f)))
         return int(f.value)
+
+    def stats(self):
+        st = _lib.Stats()
+        self._check(self._L.wrach_stats(self._ctx, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in _lib.Stats._fields_ if f != "reserved"}
+
+    def rebin_trace(self):
+        """Nanoseconds between the phase boundaries of the latest rebin."""
+        buf = (ctypes.c_uint64 * 32)()
+        cnt = ctypes.c_uint32(0)
+        self._check(self._L.wrach_rebin_trace(self._ctx, buf, 32, ctypes.byref(cnt)))
+        t = [int(buf[i]) for i in range(cnt.value)]
+        return [b - a for a, b in zip(t, t[1:])]
 
     @property
     def kernel_launches(self):

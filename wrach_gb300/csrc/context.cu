@@ -60,6 +60,17 @@ __global__ void k_gather_u32(const uint32_t* __restrict__ src,
   if (i < n) out[i] = src[idx[i]];
 }
 
+// The smallest binary32 s with sqrt_rn(s) > min_d.  Correctly rounded
+// square roots are monotonic, so for every s: s >= skip_threshold(min_d)
+// exactly when sqrtf(s) > min_d.
+float skip_threshold(float min_d) {
+  volatile float s = min_d * min_d;
+  while (s > 0.0f && std::sqrt((float)std::nextafter((float)s, 0.0f)) > min_d)
+    s = std::nextafter((float)s, 0.0f);
+  while (!(std::sqrt((float)s) > min_d)) s = std::nextafter((float)s, INFINITY);
+  return s;
+}
+
 uint32_t bits_for(uint32_t v) {
   uint32_t b = 0;
   while (b < 32 && (v >> b) != 0) ++b;
@@ -92,13 +103,15 @@ struct WrachContext {
   uint32_t *kA = nullptr, *kB = nullptr, *iA = nullptr, *iB = nullptr;
   size_t sort_cap = 0;
   uint32_t* hist = nullptr;
-  uint64_t* status = nullptr;
+  uint32_t* tile_sums = nullptr;  // one word per tile of the cell table
   uint32_t ntiles = 0;
+  uint32_t key_bits = 0, digit_bits = 0;
   Ctrl* ctrl = nullptr;
   int rebin_grid = 0;
   std::vector<Store> stores;
   float2 *stage_pos = nullptr, *stage_vel = nullptr;
   size_t stage_cap = 0;
+  uint32_t* counts = nullptr;     // per-cell counts of the rebin (ncells + 1)
   uint32_t* table_tmp = nullptr;  // one world's reference-layout table
   uint32_t* gather_idx = nullptr; // nworlds + 1
   uint32_t* gather_out = nullptr;
@@ -151,8 +164,8 @@ void release(WrachContext* ctx) {
   void* ptrs[] = {ctx->worlds_d, ctx->pos, ctx->vel, ctx->pos_o, ctx->vel_o,
                   ctx->q1, ctx->q2, ctx->cell_of[0], ctx->cell_of[1],
                   ctx->cs[0], ctx->cs[1], ctx->keys, ctx->kA, ctx->kB,
-                  ctx->iA, ctx->iB, ctx->hist, ctx->status, ctx->ctrl,
-                  ctx->stage_pos, ctx->stage_vel, ctx->table_tmp,
+                  ctx->iA, ctx->iB, ctx->hist, ctx->tile_sums, ctx->ctrl,
+                  ctx->stage_pos, ctx->stage_vel, ctx->table_tmp, ctx->counts,
                   ctx->gather_idx, ctx->gather_out};
   for (void* p : ptrs) dfree(p);
   for (auto& s : ctx->stores) {
@@ -244,15 +257,16 @@ wrach::RebinArgs rebin_args(WrachContext* ctx) {
   r.worlds = ctx->worlds_d;
   r.nworlds = (int)ctx->nworlds;
   r.ncells = ctx->ncells;
-  r.status = ctx->status;
-  r.ntiles = ctx->ntiles;
+  r.tile_sums = ctx->tile_sums;
   r.kA = ctx->kA;
   r.kB = ctx->kB;
   r.iA = ctx->iA;
   r.iB = ctx->iB;
   r.hist = ctx->hist;
-  r.key_bits = bits_for(ctx->ncells);
+  r.key_bits = ctx->key_bits;
+  r.digit_bits = ctx->digit_bits;
   r.keys = ctx->keys;
+  r.counts = ctx->counts;
   r.ctrl = ctx->ctrl;
   return r;
 }
@@ -292,7 +306,6 @@ int enqueue_frame(WrachContext* ctx) {
   wrach::RebinArgs r = rebin_args(ctx);
   r.n = ctx->n;
   r.dst_capacity = ctx->total_cap;
-  r.cs_old = ctx->cs[ctx->cur];
   r.pos_src = ctx->pos_o;
   r.vel_src = ctx->vel_o;
   r.cs_new = ctx->cs[ctx->cur ^ 1];
@@ -366,6 +379,12 @@ int world_settings_init(WorldDev& w, float width, float height, float ax,
   w.gy = (uint32_t)gy;
   w.blx = blx;
   w.bly = bly;
+  // x / gx for every x < 2^31 as (x * m) >> (31 + l), l = ceil(log2 gx),
+  // m = floor(2^(31 + l) / gx) + 1 < 2^32 (Granlund & Montgomery, 1994)
+  uint32_t l = 0;
+  while ((1ull << l) < w.gx) ++l;
+  w.div_m = (uint32_t)((1ull << (31 + l)) / w.gx + 1);
+  w.div_s = 31 + l;
   return 0;
 }
 
@@ -384,8 +403,7 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   };
   if (c.cell_size == 0) return bad("cell_size must be positive");
   if (c.mode != WRACH_MODE_REFERENCE && c.mode != WRACH_MODE_EXTENDED) return bad("unknown mode");
-  if (c.mode == WRACH_MODE_REFERENCE &&
-      (c.cell_capacity == 0 || c.cell_capacity > wrach::kMaxCellCapacity))
+  if (c.cell_capacity == 0 || c.cell_capacity > wrach::kMaxCellCapacity)
     return bad("cell_capacity must be in 1..16");
   if (!(c.min_distance > 0.0f) || !(c.max_velocity >= 0.0f)) return bad("bad physics constants");
   if (c.iterations > 64) return bad("iterations must be at most 64");
@@ -415,6 +433,7 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   ctx->ph.min_d = c.min_distance;
   ctx->ph.vmax = c.max_velocity;
   ctx->ph.cap = c.cell_capacity;
+  ctx->ph.skip_d2 = skip_threshold(c.min_distance);
 
   ctx->nworlds = nworlds;
   ctx->worlds_h.resize(nworlds);
@@ -438,12 +457,15 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
                                      : wrach_max_particles_per_frame((uint32_t)wc, c.cell_size);
     ctx->cap_h[w] = wcap;
     cap += wcap;
-    if (cells > 0xF0000000ull || cap > 0x7FFFFFFFull) return bad("grid or capacity too large");
+    // keys carry a flag in bit 31, so cell indices stay below 2^31
+    if (cells > 0x7FFFFFF0ull || cap > 0x7FFFFFFFull) return bad("grid or capacity too large");
   }
   ctx->ncells = (uint32_t)cells;
   ctx->total_cap = (uint32_t)cap;
-  ctx->ntiles = (ctx->ncells + wrach::kTileCells - 1) / wrach::kTileCells;
-  ctx->rebin_grid = wrach::rebin_grid_size(ctx->device);
+  ctx->key_bits = bits_for(ctx->ncells);
+  ctx->digit_bits = wrach::rebin_digit_bits(ctx->key_bits);
+  ctx->rebin_grid = wrach::rebin_grid_size(ctx->device, ctx->digit_bits);
+  if (c.rebin_blocks && (int)c.rebin_blocks < ctx->rebin_grid) ctx->rebin_grid = (int)c.rebin_blocks;
   if (ctx->rebin_grid <= 0) {
     int rc = fail(ctx, WRACH_ERR_CUDA, "cannot size the rebin grid (kernel image not loadable?)");
     delete ctx;
@@ -475,12 +497,16 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
     if ((e = dalloc(&ctx->cs[i], (size_t)ctx->ncells + 1)) != cudaSuccess) return oom(e);
     if ((e = cudaMemset(ctx->cs[i], 0, ((size_t)ctx->ncells + 1) * 4)) != cudaSuccess) return oom(e);
   }
-  if ((e = dalloc(&ctx->hist, (size_t)256 * ctx->rebin_grid)) != cudaSuccess) return oom(e);
-  if ((e = dalloc(&ctx->status, std::max<uint32_t>(ctx->ntiles, 1))) != cudaSuccess) return oom(e);
-  if ((e = cudaMemset(ctx->status, 0, sizeof(uint64_t) * std::max<uint32_t>(ctx->ntiles, 1))) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->hist, ((size_t)1 << ctx->digit_bits) * (ctx->rebin_grid + 1))) != cudaSuccess)
+    return oom(e);
+  // one sum per tile of kTileCells cells of the table
+  ctx->ntiles = (ctx->ncells + wrach::kTileCells - 1) / wrach::kTileCells;
+  if ((e = dalloc(&ctx->tile_sums, ctx->ntiles)) != cudaSuccess) return oom(e);
   if ((e = dalloc(&ctx->ctrl, 1)) != cudaSuccess) return oom(e);
   if ((e = cudaMemset(ctx->ctrl, 0, sizeof(Ctrl))) != cudaSuccess) return oom(e);
   if ((e = dalloc(&ctx->table_tmp, (size_t)ctx->max_world_cells + 2)) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->counts, (size_t)ctx->ncells + 1)) != cudaSuccess) return oom(e);
+  if ((e = cudaMemset(ctx->counts, 0, ((size_t)ctx->ncells + 1) * 4)) != cudaSuccess) return oom(e);
   if ((e = dalloc(&ctx->gather_idx, nworlds + 1)) != cudaSuccess) return oom(e);
   if ((e = dalloc(&ctx->gather_out, nworlds + 1)) != cudaSuccess) return oom(e);
   {
@@ -542,7 +568,6 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
   wrach::RebinArgs r = rebin_args(ctx);
   r.n = (uint32_t)nsrc;
   r.dst_capacity = ctx->total_cap;
-  r.cs_old = ctx->cs[ctx->cur];
   r.pos_src = ctx->stage_pos;
   r.vel_src = ctx->stage_vel;
   r.cs_new = ctx->cs[ctx->cur ^ 1];
@@ -766,6 +791,36 @@ int wrach_flags(WrachContext* ctx, uint32_t* flags) {
   CK(cudaMemcpyAsync(&h, ctx->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   *flags = h.flags;
+  return WRACH_OK;
+}
+
+int wrach_stats(WrachContext* ctx, WrachStats* out) {
+  if (!ctx || !out) return WRACH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(ctx->device);
+  Ctrl h{};
+  CK(cudaMemcpyAsync(&h, ctx->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::memset(out, 0, sizeof(*out));
+  out->flags = h.flags;
+  out->frames = h.frames;
+  out->overflow = h.overflow;
+  out->rebin_blocks = (uint32_t)ctx->rebin_grid;
+  out->tiles = ctx->ntiles;
+  out->particles = ctx->n;
+  out->cells = ctx->ncells;
+  return WRACH_OK;
+}
+
+int wrach_rebin_trace(WrachContext* ctx, uint64_t* ns, uint32_t cap, uint32_t* count) {
+  if (!ctx || !count) return WRACH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(ctx->device);
+  Ctrl h{};
+  CK(cudaMemcpyAsync(&h, ctx->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  uint32_t n = 0;
+  while (n < wrach::kPhaseSlots && h.phase_ns[n]) ++n;
+  *count = n;
+  for (uint32_t i = 0; i < n && i < cap && ns; ++i) ns[i] = h.phase_ns[i];
   return WRACH_OK;
 }
 

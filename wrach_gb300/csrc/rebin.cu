@@ -8,19 +8,22 @@
 // inside a cell unspecified; the CPU packer's order, spatial_bin.rs:103-149,
 // is the stable one.)
 //
-// Windowed path (every frame whose particles moved at most kMaxWindow cells):
-// the source is in old-cell order, so every particle that lands in cell k
-// comes from the (2R+1)^2 old cells around k, R = the frame's largest cell
-// displacement.  Walking those old cells in row-major order visits them in
-// source order, which gives each destination cell its count and, on a second
-// walk, each particle's stable rank.  The counts are scanned in one pass with
-// decoupled look-back over tiles of kTileCells consecutive cells, so the
-// table, the scan and the scatter take a single launch.
-//
-// General path (uploads, or a frame that moved a particle further): an LSD
-// radix sort (8-bit digits) of (key, source index) over the whole grid of
-// co-resident blocks with grid barriers, then a gather and a table built by
-// binary search.
+// The sort is an LSD radix sort (8-bit digits) of (cell key, source index),
+// run over all co-resident blocks of one cooperative launch with grid
+// barriers between its phases.  Every block owns a contiguous chunk of the
+// source, split into one contiguous sub-range per warp; a warp ranks its items
+// 32 at a time in source order with warp-private digit counters in shared
+// memory (__match_any_sync groups equal digits inside a step), so the rank of
+// every item is stable.  Per pass:
+//   A  digit histogram of each block (the warps' counters summed),
+//   B  per digit, the exclusive prefix over blocks (digit rows spread over the
+//      blocks) and the digit totals,
+//   C  each item's destination = digit offset + block offset + warp offset +
+//      rank, and the scatter.
+// The cost is the same for any cell occupancy and any particle displacement.
+// The cell-start table comes from per-cell counts (atomics during the first
+// pass): tile sums are taken between two barriers of the first pass, and after
+// the gather every block scans them and writes its own tiles' starts.
 #include <limits.h>
 
 #include "wrach_internal.cuh"
@@ -36,13 +39,9 @@ constexpr uint32_t NW = T / 32;
 
 struct SmemRebin {
   uint32_t warp_sum[NW];
-  uint32_t tile;
-  uint32_t tile_excl;
   uint32_t epoch;
-  uint32_t dmax;
   uint32_t flags;
-  uint32_t run[256];
-  uint32_t wc[NW * 256];
+  uint32_t wc[2 * kTileCells / CPT];  // tile prefixes of this block (write_table)
 };
 
 // Exclusive scan of one value per thread over the block.
@@ -102,259 +101,214 @@ __device__ void grid_barrier(Ctrl* ctrl, uint32_t& flags) {
 }
 
 // ---------------------------------------------------------------------------
-// Windowed path
+// Radix sort
 // ---------------------------------------------------------------------------
 
-// Walk the old cells within R of cells [xa, xb] of row cy (keys
-// kbase .. kbase + nk - 1) in source order.  Count mode adds to cnt[];
-// scatter mode uses cnt[] as the running destination of each cell.
-template <bool SCATTER>
-__device__ __forceinline__ void walk_row(const RebinArgs& a, const WorldDev& w,
-                                         uint32_t cy, uint32_t xa, uint32_t xb,
-                                         uint32_t kbase, uint32_t nk,
-                                         uint32_t R, uint32_t (&cnt)[CPT],
-                                         uint32_t& overflow) {
-  const uint32_t xlo = xa >= R ? xa - R : 0u;
-  const uint32_t xhi = min(xb + R, w.gx - 1);
-  const uint32_t ylo = cy >= R ? cy - R : 0u;
-  const uint32_t yhi = min(cy + R, w.gy - 1);
-  for (uint32_t row = ylo; row <= yhi; ++row) {
-    const uint32_t rb = w.cell_off + row * w.gx;
-    // clamped so that an inconsistent table can never index past the source
-    const uint32_t je = min(a.cs_old[rb + xhi + 1], a.n);
-    const uint32_t js = min(a.cs_old[rb + xlo], je);
-    for (uint32_t j = js; j < je; ++j) {
-      const uint32_t d = a.keys[j] - kbase;
-      if (d >= nk) continue;
-      if (SCATTER) {
-        uint32_t dst = 0;
-#pragma unroll
-        for (uint32_t u = 0; u < CPT; ++u)
-          if (d == u) dst = cnt[u]++;
-        if (dst < a.dst_capacity) {
-          a.pos_dst[dst] = a.pos_src[j];
-          a.vel_dst[dst] = a.vel_src[j];
-          a.cell_dst[dst] = kbase + d;
-        } else {
-          ++overflow;
-        }
-      } else {
-#pragma unroll
-        for (uint32_t u = 0; u < CPT; ++u) cnt[u] += (d == u);
-      }
-    }
-  }
+// Items of a warp are ranked in steps of 32 (lane order = source order); the
+// loads of kSeg steps are issued before they are consumed.
+constexpr uint32_t kSeg = 8;
+
+// Phase trace: block 0 records the time at each phase boundary.
+__device__ __forceinline__ void trace(const RebinArgs& a, uint32_t& slot) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && slot < kPhaseSlots)
+    a.ctrl->phase_ns[slot] = global_ns();
+  ++slot;
 }
 
-template <bool SCATTER>
-__device__ __forceinline__ void walk_cells(const RebinArgs& a, uint32_t c0,
-                                           uint32_t ncell, uint32_t R,
-                                           uint32_t (&cnt)[CPT],
-                                           uint32_t& overflow) {
-  const WorldDev w = a.worlds[world_of_cell(a.worlds, a.nworlds, c0)];
-  const uint32_t l0 = c0 - w.cell_off;
-  const uint32_t cy = l0 / w.gx, cx0 = l0 % w.gx;
-  if (cx0 + ncell <= w.gx) {
-    // all of this thread's cells sit in one row of one world: one walk
-    walk_row<SCATTER>(a, w, cy, cx0, cx0 + ncell - 1, c0, ncell, R, cnt,
-                      overflow);
-    return;
-  }
-  // the cells straddle a row (or world) boundary: one walk per cell
-#pragma unroll
-  for (uint32_t u = 0; u < CPT; ++u) {
-    if (u < ncell) {
-      const uint32_t c = c0 + u;
-      const WorldDev wu = a.worlds[world_of_cell(a.worlds, a.nworlds, c)];
-      const uint32_t l = c - wu.cell_off;
-      uint32_t one[CPT] = {};
-      one[0] = cnt[u];
-      walk_row<SCATTER>(a, wu, l / wu.gx, l % wu.gx, l % wu.gx, c, 1, R, one,
-                        overflow);
-      cnt[u] = one[0];
-    }
-  }
-}
-
-__device__ void windowed_tile(const RebinArgs& a, uint32_t tile, uint32_t R,
-                              SmemRebin& sm, uint32_t& flags,
-                              uint32_t& overflow) {
-  const uint32_t t = threadIdx.x;
-  const uint32_t c0 = tile * kTileCells + t * CPT;
-  const uint32_t ncell = c0 < a.ncells ? min(CPT, a.ncells - c0) : 0u;
-  uint32_t cnt[CPT] = {};
-  if (ncell) walk_cells<false>(a, c0, ncell, R, cnt, overflow);
-  uint32_t mine = 0;
-#pragma unroll
-  for (uint32_t u = 0; u < CPT; ++u) mine += cnt[u];
-  uint32_t agg;
-  const uint32_t excl_t = block_exclusive_scan(mine, agg, sm.warp_sum);
-
-  // decoupled look-back (warp 0)
-  if (t < 32) {
-    const uint32_t lane = t;
-    const uint64_t tag = (uint64_t)(sm.epoch & 0x3FFFFFFFu) << 34;
-    if (lane == 0)
-      st_release_u64(&a.status[tile],
-                     tag | ((tile == 0 ? 2ull : 1ull) << 32) | agg);
-    uint32_t excl = 0;
-    if (tile > 0) {
-      int64_t base = (int64_t)tile - 1;
-      while (true) {
-        const int64_t j = base - (int64_t)lane;
-        uint32_t flag = 2u, val = 0u;
-        if (j >= 0) {
-          const uint64_t t0 = global_ns();
-          uint64_t s;
-          while (true) {
-            s = ld_acquire_u64(&a.status[j]);
-            if ((s >> 34) == (tag >> 34) && ((s >> 32) & 3ull) != 0) break;
-            if (global_ns() - t0 > kWaitLimitNs) {
-              flags |= kFlagTimeout;
-              s = tag | (2ull << 32);
-              break;
-            }
-          }
-          flag = (uint32_t)((s >> 32) & 3ull);
-          val = (uint32_t)s;
-        }
-        const uint32_t pmask = __ballot_sync(0xffffffffu, flag == 2u);
-        if (pmask) {
-          const uint32_t first = __ffs(pmask) - 1;
-          excl += __reduce_add_sync(0xffffffffu, lane <= first ? val : 0u);
-          break;
-        }
-        excl += __reduce_add_sync(0xffffffffu, val);
-        base -= 32;
-      }
-      if (lane == 0)
-        st_release_u64(&a.status[tile], tag | (2ull << 32) | (excl + agg));
-    }
-    if (lane == 0) sm.tile_excl = excl;
-  }
-  __syncthreads();
-  const uint32_t tile_excl = sm.tile_excl;
-
-  uint32_t run[CPT];
-  uint32_t acc = tile_excl + excl_t;
-#pragma unroll
-  for (uint32_t u = 0; u < CPT; ++u) {
-    run[u] = acc;
-    acc += cnt[u];
-  }
-  if (ncell == CPT) {
-    *reinterpret_cast<uint4*>(a.cs_new + c0) =
-        make_uint4(run[0], run[1], run[2], run[3]);
-  } else {
-#pragma unroll
-    for (uint32_t u = 0; u < CPT; ++u)
-      if (u < ncell) a.cs_new[c0 + u] = run[u];
-  }
-  if (tile == a.ntiles - 1 && t == 0) a.cs_new[a.ncells] = tile_excl + agg;
-  if (ncell) walk_cells<true>(a, c0, ncell, R, run, overflow);
-  __syncthreads();  // smem reuse by the next tile
-}
-
-// ---------------------------------------------------------------------------
-// General path
-// ---------------------------------------------------------------------------
-
-__device__ void block_scan_inplace(uint32_t* arr, uint32_t n, SmemRebin& sm) {
-  const uint32_t t = threadIdx.x;
-  const uint32_t per = (n + T - 1) / T;
-  const uint32_t lo = min(t * per, n), hi = min(lo + per, n);
+// Sum of one tile of kTileCells per-cell counts (L2-coherent loads).
+__device__ __forceinline__ uint32_t tile_count_sum(const uint32_t* counts,
+                                                   uint32_t tile, uint32_t n,
+                                                   SmemRebin& sm) {
+  const uint32_t c0 = tile * kTileCells + threadIdx.x * CPT;
   uint32_t s = 0;
-  for (uint32_t i = lo; i < hi; ++i) s += __ldcg(arr + i);
+#pragma unroll
+  for (uint32_t u = 0; u < CPT; ++u) s += c0 + u < n ? __ldcg(counts + c0 + u) : 0u;
   uint32_t total;
-  uint32_t run = block_exclusive_scan(s, total, sm.warp_sum);
-  for (uint32_t i = lo; i < hi; ++i) {
-    const uint32_t v = __ldcg(arr + i);
-    arr[i] = run;
-    run += v;
-  }
+  block_exclusive_scan(s, total, sm.warp_sum);
+  return total;
 }
 
-__device__ __forceinline__ uint32_t lower_bound_cg(const uint32_t* a,
-                                                   uint32_t n, uint32_t key) {
-  uint32_t lo = 0, hi = n;
-  while (lo < hi) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (__ldcg(a + mid) < key)
-      lo = mid + 1;
-    else
-      hi = mid;
+// The cell-start table from the per-cell counts: every block scans the tile
+// sums (each block reads all of them) for the prefixes of its own tiles,
+// then writes its tiles' starts and zeroes their counts for the next launch.
+__device__ void write_table(const RebinArgs& a, SmemRebin& sm) {
+  const uint32_t t = threadIdx.x, n = a.ncells;
+  const uint32_t ntiles = (n + kTileCells - 1) / kTileCells;
+  const uint32_t per = (ntiles + T - 1) / T;
+  const uint32_t i0 = min(t * per, ntiles), i1 = min(i0 + per, ntiles);
+  uint32_t s = 0;
+  for (uint32_t i = i0; i < i1; ++i) s += __ldcg(a.tile_sums + i);
+  uint32_t total;
+  const uint32_t excl = block_exclusive_scan(s, total, sm.warp_sum);
+  // this block's tiles, kOwn at a time: their prefixes into shared memory,
+  // then their starts
+  constexpr uint32_t kOwn = sizeof(sm.wc) / sizeof(sm.wc[0]);
+  const uint32_t G = gridDim.x, mine = ntiles > blockIdx.x ? (ntiles - blockIdx.x + G - 1) / G : 0u;
+  for (uint32_t o0 = 0; o0 < mine; o0 += kOwn) {
+    uint32_t run = excl;
+    for (uint32_t i = i0; i < i1; ++i) {
+      if (i % G == blockIdx.x && i / G >= o0 && i / G < o0 + kOwn) sm.wc[i / G - o0] = run;
+      run += __ldcg(a.tile_sums + i);
+    }
+    __syncthreads();
+    for (uint32_t o = o0; o < min(mine, o0 + kOwn); ++o) {
+      const uint32_t tile = blockIdx.x + o * G;
+      const uint32_t c0 = tile * kTileCells + t * CPT;
+      uint32_t v[CPT];
+#pragma unroll
+      for (uint32_t u = 0; u < CPT; ++u) v[u] = c0 + u < n ? __ldcg(a.counts + c0 + u) : 0u;
+      uint32_t agg;
+      uint32_t acc = sm.wc[o - o0] + block_exclusive_scan(v[0] + v[1] + v[2] + v[3], agg, sm.warp_sum);
+#pragma unroll
+      for (uint32_t u = 0; u < CPT; ++u) {
+        if (c0 + u < n) {
+          a.cs_new[c0 + u] = acc;
+          a.counts[c0 + u] = 0;
+        }
+        acc += v[u];
+      }
+    }
+    __syncthreads();
   }
-  return lo;
+  if (blockIdx.x == 0 && t == 0) a.cs_new[n] = total;
 }
 
-__device__ void general_sort(const RebinArgs& a, SmemRebin& sm,
-                             uint32_t& flags, uint32_t& overflow) {
+// LSD radix sort of (key, source index) by key, stable, `a.digit_bits` bits
+// per pass; the warp-private digit counters live in dynamic shared memory
+// (NW * 2^digit_bits words).
+__device__ void radix_sort(const RebinArgs& a, SmemRebin& sm, uint32_t* wcd,
+                           uint32_t& flags, uint32_t& overflow) {
   const uint32_t G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
   const uint32_t lane = t & 31, warp = t >> 5;
-  const uint32_t n = a.n;
-  const uint32_t chunk = ((n + G - 1) / G + T - 1) / T * T;
-  const uint32_t lo = min(b * chunk, n), hi = min(lo + chunk, n);
-  const uint32_t passes = a.key_bits ? (a.key_bits + 7) / 8 : 1u;
   const uint32_t lanemask_lt = (1u << lane) - 1u;
+  const uint32_t n = a.n;
+  const uint32_t chunk = (n + G - 1) / G;
+  const uint32_t blo = min(b * chunk, n), bhi = min(blo + chunk, n);
+  const uint32_t wsz = (bhi - blo + NW - 1) / NW;
+  const uint32_t wlo = min(blo + warp * wsz, bhi), whi = min(wlo + wsz, bhi);
+  const uint32_t DB = a.digit_bits, RADIX = 1u << DB, MASK = RADIX - 1u;
+  const uint32_t passes = (a.key_bits + DB - 1) / DB;
+  const uint32_t ntiles = (a.ncells + kTileCells - 1) / kTileCells;
+  uint32_t* tot = a.hist + RADIX * G;
+  uint32_t* wc = wcd + warp * RADIX;
+  uint32_t slot = 0;
+  trace(a, slot);
 
   for (uint32_t p = 0; p < passes; ++p) {
-    const uint32_t shift = 8 * p;
+    const uint32_t shift = DB * p;
     const uint32_t* sk = p == 0 ? a.keys : ((p & 1) ? a.kA : a.kB);
     const uint32_t* si = p == 0 ? nullptr : ((p & 1) ? a.iA : a.iB);
     uint32_t* dk = (p & 1) ? a.kB : a.kA;
     uint32_t* di = (p & 1) ? a.iB : a.iA;
 
-    // digit histogram of this block's chunk
-    sm.run[t] = 0;
+    // A: digit histogram (warp-private counters); on the first pass also the
+    // per-cell counts of the table
+    for (uint32_t k = t; k < NW * RADIX; k += T) wcd[k] = 0;
     __syncthreads();
-    for (uint32_t i = lo + t; i < hi; i += T)
-      atomicAdd(&sm.run[(__ldcg(sk + i) >> shift) & 255u], 1u);
-    __syncthreads();
-    a.hist[t * G + b] = sm.run[t];
-    grid_barrier(a.ctrl, flags);
-
-    // digit-major exclusive scan of all blocks' histograms
-    if (b == 0) block_scan_inplace(a.hist, 256 * G, sm);
-    grid_barrier(a.ctrl, flags);
-
-    // stable scatter, sub-tiles of T items in source order
-    sm.run[t] = __ldcg(a.hist + t * G + b);
-    __syncthreads();
-    for (uint32_t base = lo; base < hi; base += T) {
-      const uint32_t i = base + t;
-      const bool valid = i < hi;
-      const uint32_t key = valid ? __ldcg(sk + i) : 0u;
-      const uint32_t idx = valid ? (si ? __ldcg(si + i) : i) : 0u;
-      const uint32_t d = valid ? (key >> shift) & 255u : 256u;
-      const uint32_t peers = __match_any_sync(0xffffffffu, d);
-      const uint32_t rank = __popc(peers & lanemask_lt);
-      for (uint32_t k = t; k < NW * 256; k += T) sm.wc[k] = 0;
-      __syncthreads();
-      if (valid && rank == 0) sm.wc[warp * 256 + d] = __popc(peers);
-      __syncthreads();
-      {
-        uint32_t run = sm.run[t];
+    for (uint32_t base = wlo; base < whi; base += 32 * kSeg) {
+      uint32_t key[kSeg];
 #pragma unroll
-        for (uint32_t w = 0; w < NW; ++w) {
-          const uint32_t c = sm.wc[w * 256 + t];
-          sm.wc[w * 256 + t] = run;
-          run += c;
-        }
-        sm.run[t] = run;
+      for (uint32_t u = 0; u < kSeg; ++u) {
+        const uint32_t i = base + 32 * u + lane;
+        key[u] = i < whi ? __ldcg(sk + i) : 0xFFFFFFFFu;
       }
-      __syncthreads();
-      if (valid) {
-        const uint32_t dst = sm.wc[warp * 256 + d] + rank;
-        if (dst < n) {  // always true unless a barrier timed out
-          dk[dst] = key;
-          di[dst] = idx;
-        }
+#pragma unroll
+      for (uint32_t u = 0; u < kSeg; ++u) {
+        const bool valid = key[u] != 0xFFFFFFFFu;
+        if (p == 0 && valid && key[u] < a.ncells) atomicAdd(&a.counts[key[u]], 1u);
+        const uint32_t d = valid ? (key[u] >> shift) & MASK : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        if (valid && (peers & lanemask_lt) == 0) wc[d] += __popc(peers);
+        __syncwarp();
       }
-      __syncthreads();
     }
+    __syncthreads();
+    for (uint32_t d = t; d < RADIX; d += T) {
+      uint32_t h = 0;
+      for (uint32_t w = 0; w < NW; ++w) h += wcd[w * RADIX + d];
+      a.hist[d * G + b] = h;
+    }
+    trace(a, slot);
     grid_barrier(a.ctrl, flags);
+    trace(a, slot);
+
+    // B: per digit, exclusive prefix over the blocks and the digit total;
+    // on the first pass also the tile sums of the per-cell counts
+    for (uint32_t d = b; d < RADIX; d += G) {
+      const uint32_t per = (G + T - 1) / T;
+      const uint32_t i0 = min(t * per, G), i1 = min(i0 + per, G);
+      uint32_t s = 0;
+      for (uint32_t i = i0; i < i1; ++i) s += __ldcg(a.hist + d * G + i);
+      uint32_t total;
+      uint32_t run = block_exclusive_scan(s, total, sm.warp_sum);
+      for (uint32_t i = i0; i < i1; ++i) {
+        const uint32_t v = __ldcg(a.hist + d * G + i);
+        a.hist[d * G + i] = run;
+        run += v;
+      }
+      if (t == 0) tot[d] = total;
+    }
+    if (p == 0)
+      for (uint32_t tile = b; tile < ntiles; tile += G) {
+        const uint32_t s = tile_count_sum(a.counts, tile, a.ncells, sm);
+        if (t == 0) a.tile_sums[tile] = s;
+      }
+    trace(a, slot);
+    grid_barrier(a.ctrl, flags);
+    trace(a, slot);
+
+    // C: running destinations of each (warp, digit), then the stable scatter
+    {
+      const uint32_t dpt = (RADIX + T - 1) / T;  // digits per thread
+      const uint32_t d0 = min(t * dpt, RADIX), d1 = min(d0 + dpt, RADIX);
+      uint32_t s = 0;
+      for (uint32_t d = d0; d < d1; ++d) s += __ldcg(tot + d);
+      uint32_t total;
+      uint32_t doff = block_exclusive_scan(s, total, sm.warp_sum);
+      for (uint32_t d = d0; d < d1; ++d) {
+        uint32_t off = doff + __ldcg(a.hist + d * G + b);
+        doff += __ldcg(tot + d);
+        for (uint32_t w = 0; w < NW; ++w) {
+          const uint32_t c = wcd[w * RADIX + d];
+          wcd[w * RADIX + d] = off;
+          off += c;
+        }
+      }
+    }
+    __syncthreads();
+    for (uint32_t base = wlo; base < whi; base += 32 * kSeg) {
+      uint32_t key[kSeg], idx[kSeg];
+#pragma unroll
+      for (uint32_t u = 0; u < kSeg; ++u) {
+        const uint32_t i = base + 32 * u + lane;
+        key[u] = i < whi ? __ldcg(sk + i) : 0xFFFFFFFFu;
+        idx[u] = i < whi ? (si ? __ldcg(si + i) : i) : 0u;
+      }
+#pragma unroll
+      for (uint32_t u = 0; u < kSeg; ++u) {
+        const bool valid = key[u] != 0xFFFFFFFFu;
+        const uint32_t d = valid ? (key[u] >> shift) & MASK : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t start = valid ? wc[d] : 0u;
+        __syncwarp();
+        if (valid) {
+          const uint32_t rank = __popc(peers & lanemask_lt);
+          if ((peers >> lane) == 1u) wc[d] = start + __popc(peers);
+          const uint32_t dst = start + rank;
+          if (dst < n) {  // always true unless a barrier timed out
+            dk[dst] = key[u];
+            di[dst] = idx[u];
+          }
+        }
+        __syncwarp();
+      }
+    }
+    trace(a, slot);
+    grid_barrier(a.ctrl, flags);
+    trace(a, slot);
   }
 
+  // gather into cell order, then the table
   const uint32_t last = passes - 1;
   const uint32_t* sk = (last & 1) ? a.kB : a.kA;
   const uint32_t* si = (last & 1) ? a.iB : a.iA;
@@ -370,40 +324,24 @@ __device__ void general_sort(const RebinArgs& a, SmemRebin& sm,
       ++overflow;
     }
   }
-  for (uint32_t c = b * T + t; c <= a.ncells; c += G * T)
-    a.cs_new[c] = lower_bound_cg(sk, n, c);
+  trace(a, slot);
+  write_table(a, sm);
+  trace(a, slot);
 }
 
-__global__ void __launch_bounds__(T) k_rebin(RebinArgs a) {
+__global__ void __launch_bounds__(T, 3) k_rebin(RebinArgs a) {
   __shared__ SmemRebin sm;
+  extern __shared__ uint32_t wcd[];
   const uint32_t t = threadIdx.x;
   uint32_t flags = 0, overflow = 0;
   if (t == 0) {
     sm.epoch = ld_acquire_u32(&a.ctrl->epoch);
-    sm.dmax = ld_acquire_u32(&a.ctrl->dmax);
     sm.flags = 0;
   }
   __syncthreads();
-  const uint32_t R = sm.dmax;
-  const bool general = a.force_general || R > kMaxWindow;
-  if (general) {
-    if (!a.force_general && blockIdx.x == 0 && t == 0) {
-      atomicAdd(&a.ctrl->general, 1u);
-      flags |= kFlagGeneralSort;
-    }
-    general_sort(a, sm, flags, overflow);
-  } else {
-    while (true) {
-      if (t == 0) sm.tile = atomicAdd(&a.ctrl->ticket, 1u);
-      __syncthreads();
-      const uint32_t tile = sm.tile;
-      __syncthreads();
-      if (tile >= a.ntiles) break;
-      windowed_tile(a, tile, R, sm, flags, overflow);
-    }
-  }
+  radix_sort(a, sm, wcd, flags, overflow);
   // flags and overflow of the block, then the exit protocol: the last block
-  // out resets the per-launch counters and advances the epoch.
+  // out counts the launch.
   const uint32_t wf = warp_or_u32(flags);
   const uint32_t wo = __reduce_add_sync(0xffffffffu, overflow);
   if ((t & 31) == 0) {
@@ -416,14 +354,54 @@ __global__ void __launch_bounds__(T) k_rebin(RebinArgs a) {
     __threadfence();
     const uint32_t done = atomicAdd(&a.ctrl->exit_count, 1u);
     if (done == gridDim.x - 1) {
-      atomicExch(&a.ctrl->ticket, 0u);
-      atomicExch(&a.ctrl->dmax, 0u);
+      if (!a.force_general) a.ctrl->frames += 1;
       atomicExch(&a.ctrl->exit_count, 0u);
       __threadfence();
       st_release_u32(&a.ctrl->epoch, sm.epoch + 1);
     }
   }
 }
+
+}  // namespace
+
+uint32_t rebin_digit_bits(uint32_t key_bits) {
+  const uint32_t kb = key_bits ? key_bits : 1u;
+  const uint32_t passes = (kb + kMaxDigitBits - 1) / kMaxDigitBits;
+  return (kb + passes - 1) / passes;
+}
+
+size_t rebin_dynamic_smem(uint32_t digit_bits) {
+  return (size_t)NW * ((size_t)1 << digit_bits) * sizeof(uint32_t);
+}
+
+int rebin_grid_size(int device, uint32_t digit_bits) {
+  const size_t dyn = rebin_dynamic_smem(digit_bits);
+  if (cudaFuncSetAttribute(k_rebin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) !=
+      cudaSuccess)
+    return 0;
+  int sms = 0, per_sm = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rebin, T, dyn) != cudaSuccess)
+    return 0;
+  return sms * per_sm;
+}
+
+cudaError_t launch_rebin(const RebinArgs& a, int grid, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(T);
+  cfg.dynamicSmemBytes = rebin_dynamic_smem(a.digit_bits);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_rebin, a);
+}
+
+namespace {
 
 // SpatialBin::get_cell_coord (runners/bevy/src/spatial_bin.rs:48-64):
 // Rust's f32::div_euclid then a saturating `as i32` (NaN -> 0).
@@ -469,31 +447,6 @@ __global__ void k_world_table(const uint32_t* __restrict__ cell_start,
 }
 
 }  // namespace
-
-int rebin_grid_size(int device) {
-  int sms = 0, per_sm = 0;
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) !=
-      cudaSuccess)
-    return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rebin, T, 0) !=
-      cudaSuccess)
-    return 0;
-  return sms * per_sm;
-}
-
-cudaError_t launch_rebin(const RebinArgs& a, int grid, cudaStream_t st) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3(T);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeCooperative;
-  attr[0].val.cooperative = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_rebin, a);
-}
 
 cudaError_t launch_upload_keys(const WorldDev* worlds, int nworlds,
                                uint32_t ncells, uint32_t target,

@@ -1,7 +1,6 @@
 // Solve kernels: the collision/constraint pass plus the fused
 // integrate + boundary + velocity-clamp epilogue, which also emits each
-// particle's next cell key for the rebin and the largest cell displacement of
-// the frame (the rebin's window radius).
+// particle's next cell key for the rebin.
 //
 // Reference-mode kernel: one thread per cell, the sequential sweep of
 // World::physics_for_cell (shaders/physics/src/cell.rs:52-95).
@@ -14,26 +13,18 @@ namespace wrach {
 
 namespace {
 
-__device__ __forceinline__ void emit_key(const WorldDev& w, uint32_t ocx,
-                                         uint32_t ocy, float px, float py,
-                                         uint32_t& key, uint32_t& disp,
-                                         uint32_t& flags) {
-  uint32_t ncx = axis_cell(px, w.ax, w.cs, w.gx, flags);
-  uint32_t ncy = axis_cell(py, w.ay, w.cs, w.gy, flags);
-  key = w.cell_off + ncy * w.gx + ncx;
-  uint32_t dx = ncx > ocx ? ncx - ocx : ocx - ncx;
-  uint32_t dy = ncy > ocy ? ncy - ocy : ocy - ncy;
-  disp = max(disp, max(dx, dy));
+// Next cell of a solved particle (assets/shaders/particles_per_cell.wgsl:
+// 14-27), the key the rebin sorts by.
+__device__ __forceinline__ uint32_t next_key(const WorldDev& w, float px,
+                                             float py, uint32_t& flags) {
+  const uint32_t ncx = axis_cell(px, w.ax, w.cs, w.gx, flags);
+  const uint32_t ncy = axis_cell(py, w.ay, w.cs, w.gy, flags);
+  return w.cell_off + ncy * w.gx + ncx;
 }
 
-__device__ __forceinline__ void publish_frame_stats(Ctrl* ctrl, uint32_t disp,
-                                                    uint32_t flags) {
-  uint32_t wd = warp_max_u32(disp);
-  uint32_t wf = warp_or_u32(flags);
-  if ((threadIdx.x & 31) == 0) {
-    if (wd) atomicMax(&ctrl->dmax, wd);
-    if (wf) atomicOr(&ctrl->flags, wf);
-  }
+__device__ __forceinline__ void publish_flags(Ctrl* ctrl, uint32_t flags) {
+  const uint32_t wf = warp_or_u32(flags);
+  if ((threadIdx.x & 31) == 0 && wf) atomicOr(&ctrl->flags, wf);
 }
 
 // Reference mode, one thread per global cell.
@@ -52,11 +43,9 @@ k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
                   float2* __restrict__ pout, float2* __restrict__ vout,
                   uint32_t* __restrict__ keys, Ctrl* ctrl) {
   uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t disp = 0, flags = 0;
+  uint32_t flags = 0;
   if (c < ncells) {
     const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
-    const uint32_t local = c - w.cell_off;
-    const uint32_t ocx = local % w.gx, ocy = local / w.gx;
     const uint32_t s = cell_start[c], e = cell_start[c + 1];
     const uint32_t m = min(e - s, ph.cap);
     float px[kMaxCellCapacity], py[kMaxCellCapacity];
@@ -69,7 +58,7 @@ k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
       for (uint32_t j = i + 1; j < m; ++j) {
         float f;
         if (!push_factor(__fsub_rn(px[i], px[j]), __fsub_rn(py[i], py[j]),
-                         ph.min_d, f))
+                         ph.min_d, ph.skip_d2, f))
           continue;
         float dx = __fmul_rn(__fsub_rn(px[j], px[i]), f);
         float dy = __fmul_rn(__fsub_rn(py[j], py[i]), f);
@@ -82,7 +71,7 @@ k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
       enforce_limits(w, ph.vmax, qx, qy, ux, uy);
       pout[s + i] = make_float2(qx, qy);
       vout[s + i] = make_float2(ux, uy);
-      emit_key(w, ocx, ocy, qx, qy, keys[s + i], disp, flags);
+      keys[s + i] = next_key(w, qx, qy, flags);
     }
     for (uint32_t i = s + m; i < e; ++i) {
       float2 p = pin[i], v = vin[i];
@@ -91,16 +80,19 @@ k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
       enforce_limits(w, ph.vmax, qx, qy, ux, uy);
       pout[i] = make_float2(qx, qy);
       vout[i] = make_float2(ux, uy);
-      emit_key(w, ocx, ocy, qx, qy, keys[i], disp, flags);
+      keys[i] = next_key(w, qx, qy, flags);
     }
   }
-  publish_frame_stats(ctrl, disp, flags);
+  publish_flags(ctrl, flags);
 }
 
-// Extended mode, one Jacobi iteration, one thread per particle.  The
-// neighbour order is fixed (3x3 cells in row-major order, table order inside
-// a row), so the sum is deterministic.  FINAL fuses gravity, integration,
-// boundaries, the velocity clamp and the key emission.
+// Extended mode, one Jacobi iteration, one thread per particle.  As in the
+// reference (cell.rs:29-30, 79-95) only the first `cap` particles of a cell
+// take part in the pushes, as pushed particles and as neighbours; the rest of
+// an over-full cell keep their position.  The neighbour order is fixed (3x3
+// cells in row-major order, table order inside a cell), so the sum is
+// deterministic.  FINAL fuses gravity, integration, boundaries, the velocity
+// clamp and the key emission.
 template <bool FINAL>
 __global__ void __launch_bounds__(256)
 k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
@@ -109,28 +101,72 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
          float2* __restrict__ qout, const float2* __restrict__ vin,
          float2* __restrict__ vout, uint32_t* __restrict__ keys, Ctrl* ctrl) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t disp = 0, flags = 0;
+  uint32_t flags = 0;
   if (i < n) {
     const uint32_t c = cell_of[i];
     const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
-    const uint32_t local = c - w.cell_off;
-    const uint32_t cx = local % w.gx, cy = local / w.gx;
+    uint32_t cx, cy;
+    cell_xy(w, c - w.cell_off, cx, cy);
     const float2 qi = qin[i];
     float ax = 0.0f, ay = 0.0f;
-    if (do_push) {
+    if (do_push && i - cell_start[c] < ph.cap) {
+      // the table entries of the three neighbour rows first: independent
+      // loads, so their latencies overlap
       const uint32_t x0 = cx > 0 ? cx - 1 : 0;
       const uint32_t x1 = cx + 1 < w.gx ? cx + 1 : w.gx - 1;
-      const uint32_t y0 = cy > 0 ? cy - 1 : 0;
-      const uint32_t y1 = cy + 1 < w.gy ? cy + 1 : w.gy - 1;
-      for (uint32_t ny = y0; ny <= y1; ++ny) {
-        const uint32_t rb = w.cell_off + ny * w.gx;
-        const uint32_t js = cell_start[rb + x0], je = cell_start[rb + x1 + 1];
-        for (uint32_t j = js; j < je; ++j) {
-          if (j == i) continue;
+      uint32_t st[3][4];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const int ny = (int)cy - 1 + r;
+        const bool row_ok = ny >= 0 && ny < (int)w.gy;
+        const uint32_t rb = w.cell_off + (uint32_t)(row_ok ? ny : 0) * w.gx + x0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          st[r][k] = (row_ok && x0 + k <= x1 + 1) ? cell_start[rb + k] : 0u;
+      }
+      const uint32_t ncol = x1 - x0 + 1;  // 2 or 3 cells per row
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        // the row's taking-part candidates: up to three cells of at most
+        // `cap` particles each, at most 3 * kMaxCellCapacity <= 48 of them
+        const uint32_t s0 = st[r][0], s1 = st[r][1], s2 = st[r][2], s3 = st[r][3];
+        const uint32_t e0 = min(s1, s0 + ph.cap);
+        const uint32_t e1 = min(s2, s1 + ph.cap);
+        const uint32_t e2 = ncol == 3 ? min(s3, s2 + ph.cap) : s2;
+        // pass 1: which candidates are within reach (cheap, every lane); a
+        // NaN distance counts as within reach, as in the reference's test
+        static_assert(kMaxCellCapacity <= 16, "16 mask bits per cell");
+        uint64_t close = 0;
+        uint32_t k = 0;
+        for (uint32_t j = s0; j < e0; ++j, ++k) {
+          const float2 qj = qin[j];
+          const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
+          if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
+            close |= 1ull << k;
+        }
+        k = 16;
+        for (uint32_t j = s1; j < e1; ++j, ++k) {
+          const float2 qj = qin[j];
+          const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
+          if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
+            close |= 1ull << k;
+        }
+        k = 32;
+        for (uint32_t j = s2; j < e2; ++j, ++k) {
+          const float2 qj = qin[j];
+          const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
+          if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
+            close |= 1ull << k;
+        }
+        // pass 2: the reference's push for those, in candidate order
+        while (close) {
+          const uint32_t b = __ffsll((long long)close) - 1;
+          close &= close - 1;
+          const uint32_t j = (b < 16 ? s0 : (b < 32 ? s1 - 16 : s2 - 32)) + b;
           const float2 qj = qin[j];
           const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
           float f;
-          if (!push_factor(dx, dy, ph.min_d, f)) continue;
+          if (!push_factor(dx, dy, ph.min_d, ph.skip_d2, f)) continue;
           ax = __fadd_rn(ax, __fmul_rn(dx, f));
           ay = __fadd_rn(ay, __fmul_rn(dy, f));
         }
@@ -146,10 +182,10 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
       enforce_limits(w, ph.vmax, px, py, ux, uy);
       qout[i] = make_float2(px, py);
       vout[i] = make_float2(ux, uy);
-      emit_key(w, cx, cy, px, py, keys[i], disp, flags);
+      keys[i] = next_key(w, px, py, flags);
     }
   }
-  if (FINAL) publish_frame_stats(ctrl, disp, flags);
+  if (FINAL) publish_flags(ctrl, flags);
 }
 
 }  // namespace

@@ -23,6 +23,8 @@ struct WorldDev {
   float x1, y1;        // anchor + dimensions, summed in binary32 as
                        // Particle::enforce_boundaries does (particle.rs:47-52)
   int32_t blx, bly;    // cell coordinate of the grid's bottom-left cell
+  uint32_t div_m;      // x / gx == (x * div_m) >> div_s for all x < 2^31
+  uint32_t div_s;
 };
 
 struct PhysDev {
@@ -32,35 +34,41 @@ struct PhysDev {
   float min_d;
   float vmax;
   uint32_t cap;         // reference cell capacity
+  float skip_d2;        // smallest squared distance s with sqrt_rn(s) > min_d
 };
 
-// Device control block: counters for the persistent rebin kernel, the solve's
-// displacement bound and the sticky flags.  Zeroed at create; every launch of
-// the rebin kernel leaves ticket/exit_count/dmax at zero again.
+// Device control block: counters of the persistent rebin kernel and the
+// sticky flags.  Zeroed at create; every launch of the rebin kernel leaves
+// exit_count at zero again.
 struct Ctrl {
-  uint32_t ticket;      // next windowed tile
   uint32_t exit_count;  // rebin blocks finished in this launch
   uint32_t epoch;       // rebin launch counter, tags the tile status words
-  uint32_t dmax;        // max cell displacement seen by the last solve
   uint32_t flags;       // sticky WRACH_FLAG_* bits
   uint32_t bar_count;   // grid barrier arrivals
   uint32_t bar_gen;     // grid barrier generation
-  uint32_t general;     // frames that took the general re-sort
   uint32_t overflow;    // particles dropped for lack of destination room
-  uint32_t pad[7];
+  uint32_t frames;      // rebin launches that were frames (not uploads)
+  uint32_t pad[9];
+  // %globaltimer at the phase boundaries of the latest rebin launch, taken
+  // by block 0 (phase trace; kPhaseSlots entries, unused ones zero)
+  uint64_t phase_ns[32];
 };
+constexpr uint32_t kPhaseSlots = 32;
 
 constexpr uint32_t kFlagOutOfGrid = 1u;
 constexpr uint32_t kFlagNaN = 2u;
 constexpr uint32_t kFlagTimeout = 4u;
-constexpr uint32_t kFlagGeneralSort = 8u;
 
-// Largest per-frame cell displacement the windowed rebin handles; a frame
-// that moves any particle further is re-sorted by the general path.
-constexpr uint32_t kMaxWindow = 3;
 
 // Maximum reference-mode cell capacity held in registers/local memory.
 constexpr uint32_t kMaxCellCapacity = 16;
+
+// (row, column) of a world-local cell index without a hardware division.
+__device__ __forceinline__ void cell_xy(const WorldDev& w, uint32_t local,
+                                        uint32_t& cx, uint32_t& cy) {
+  cy = (uint32_t)(((uint64_t)local * w.div_m) >> w.div_s);
+  cx = local - cy * w.gx;
+}
 
 // World of a global cell index: the last world whose cell_off <= c.
 __device__ __forceinline__ int world_of_cell(const WorldDev* __restrict__ W,
@@ -112,9 +120,14 @@ __device__ __forceinline__ void enforce_limits(const WorldDev& w, float vmax,
 // The reference's pair push factor (shaders/physics/src/particles.rs:62-93):
 // returns false when the pair is farther apart than min_d, otherwise the
 // force 0.5 * (min_d - d) / d with d == 0 replaced by 0.0001.
+// `skip_d2` is the smallest binary32 s with sqrt_rn(s) > min_d (computed on
+// the host); since sqrt_rn is monotonic, s >= skip_d2 is exactly the
+// reference's `distance > MIN_DISTANCE`, decided without the square root.
 __device__ __forceinline__ bool push_factor(float ex, float ey, float min_d,
-                                            float& f) {
-  float d = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
+                                            float skip_d2, float& f) {
+  const float s = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+  if (s >= skip_d2) return false;
+  float d = __fsqrt_rn(s);
   if (d > min_d) return false;
   if (d == 0.0f) d = 0.0001f;
   f = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(min_d, d)), d);

@@ -29,8 +29,8 @@ cudaError_t launch_solve_extended(const SolveArgs& a, const float2* qin,
                                   float2* qout, bool final_pass, int do_push,
                                   cudaStream_t st);
 
-// Rebin: stable counting sort of `n` source particles by key into cell
-// order, writing a fresh cell-start table.  Persistent cooperative kernel.
+// Rebin: stable sort of `n` source particles by key into cell order, writing
+// a fresh cell-start table.  Persistent cooperative kernel.
 struct RebinArgs {
   const WorldDev* worlds;
   int nworlds;
@@ -38,22 +38,22 @@ struct RebinArgs {
   uint32_t n;                   // source particles
   uint32_t dst_capacity;        // room in pos_dst/vel_dst/cell_dst
   const uint32_t* keys;         // n source keys, ncells = leave out
-  const uint32_t* cs_old;       // old table (windowed path)
   const float2* pos_src;
   const float2* vel_src;
   uint32_t* cs_new;             // ncells + 1
   float2* pos_dst;
   float2* vel_dst;
   uint32_t* cell_dst;
-  uint64_t* status;             // one word per tile
-  uint32_t ntiles;
-  uint32_t* kA;                 // general path scratch, n each
+  uint32_t* tile_sums;          // one word per tile of kTileCells cells
+  uint32_t* kA;                 // radix sort ping-pong buffers, n each
   uint32_t* kB;
   uint32_t* iA;
   uint32_t* iB;
-  uint32_t* hist;               // 256 * grid
+  uint32_t* hist;               // 2^digit_bits * (grid + 1)
   uint32_t key_bits;
-  int force_general;
+  uint32_t digit_bits;          // rebin_digit_bits(key_bits)
+  int force_general;            // set for uploads (not counted as frames)
+  uint32_t* counts;             // ncells + 1 zeros on entry and on exit
   Ctrl* ctrl;
 };
 
@@ -61,8 +61,14 @@ constexpr uint32_t kRebinThreads = 256;
 constexpr uint32_t kCellsPerThread = 4;
 constexpr uint32_t kTileCells = kRebinThreads * kCellsPerThread;
 
+// Radix digits of at most kMaxDigitBits bits, as few passes as that allows
+// (8-bit digits measured faster than 11-bit ones on the 1M-particle frame:
+// the per-digit scans and offsets grow with the radix).
+constexpr uint32_t kMaxDigitBits = 8;
+uint32_t rebin_digit_bits(uint32_t key_bits);
+size_t rebin_dynamic_smem(uint32_t digit_bits);
 // Blocks the cooperative rebin kernel launches with on `device`.
-int rebin_grid_size(int device);
+int rebin_grid_size(int device, uint32_t digit_bits);
 cudaError_t launch_rebin(const RebinArgs& a, int grid, cudaStream_t st);
 
 // Keys for an upload re-pack: the first n_keep sources are particles of the
