@@ -120,6 +120,29 @@ int wrach_add_particles_device(WrachContext *ctx, uint32_t world,
                                const float *d_pos, const float *d_vel,
                                uint32_t n);
 
+/* Packs n particles (device arrays of n float pairs, any order) into the
+ * cell order of the world `config` describes (width, height, anchor,
+ * cell_size, device), writing d_pos_out/d_vel_out (out_capacity float pairs
+ * each) and d_indices (grid cells + 2 u32, the reference's table; its last
+ * entry is the number of particles in the frame).  The same result as
+ * wrach_set_particles followed by wrach_read, for callers that cannot
+ * allocate GPU memory (code inside a host callback or a real-time loop that
+ * must not wait on the allocator, a plugin whose host owns all device memory,
+ * a process with no memory to spare): this call allocates nothing and
+ * calls no allocating routine.  Its temporaries live in one static device
+ * array sized for at most 131,072 particles and 524,288 grid cells (about
+ * 6.3 MB on every GPU that loads the library, until exit); larger inputs
+ * return WRACH_ERR_CAPACITY.  Particles past out_capacity are not written.
+ * The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress), so make it before any stream capture.  Every call
+ * shares the array: calls that overlap on the GPU race, so keep them on one
+ * stream.  Asynchronous on `stream` (a cudaStream_t, NULL = the legacy
+ * default stream).  No counterpart in the reference. */
+int wrach_pack_noalloc(const WrachConfig *config, const float *d_pos,
+                       const float *d_vel, uint32_t n, float *d_pos_out,
+                       float *d_vel_out, uint32_t out_capacity,
+                       uint32_t *d_indices, void *stream);
+
 /* nsteps frames of the physics pass list (builder.rs:86-89): solve, count,
  * scan, pack.  Asynchronous on the context's stream. */
 int wrach_step(WrachContext *ctx, uint32_t nsteps);

@@ -88,6 +88,8 @@ SIGNATURES = {
     "wrach_set_particles": (ctypes.c_int, [_P, ctypes.c_uint32, _F, _F, ctypes.c_uint32]),
     "wrach_profile_frame": (ctypes.c_int, [_P, _F, ctypes.c_uint32, _U]),
     "wrach_add_particles_device": (ctypes.c_int, [_P, ctypes.c_uint32, _P, _P, ctypes.c_uint32]),
+    "wrach_pack_noalloc": (ctypes.c_int, [ctypes.POINTER(Config), _P, _P, ctypes.c_uint32, _P, _P,
+                                          ctypes.c_uint32, _P, _P]),
     "wrach_step": (ctypes.c_int, [_P, ctypes.c_uint32]),
     "wrach_read": (ctypes.c_int, [_P, ctypes.c_uint32, _F, _F, _U, ctypes.c_uint32]),
     "wrach_tick": (ctypes.c_int, [_P, ctypes.c_uint32, _F, _F, _U, ctypes.c_uint32]),
