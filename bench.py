@@ -63,6 +63,16 @@ def workload():
     return dims, pos, vel, cfg, desc
 
 
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/ncu_traffic.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f)["dram_bytes_per_launch"].get(kernel)
+    except Exception:
+        return None
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -325,7 +335,8 @@ def run_ours(args):
                        parallelism="replicas" if world > 1 else "single GPU"),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None,
+                     "traffic": ncu_traffic(dom),
+                     "traffic_source": "profiles/ncu_traffic.json (ncu dram__bytes_read+write, one launch)",
                      "algorithmic_bytes_per_launch": launch_bytes(dom, n, cells)},
         "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
                           "achieved": step_bytes / (max_ms / args.steps / 1000.0) / 1e9,
