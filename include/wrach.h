@@ -75,7 +75,9 @@ typedef struct WrachConfig {
   uint32_t capacity;       /* 0 = max_particles_per_frame of the grid */
   int32_t device;          /* CUDA ordinal (default 0) */
   uint32_t rebin_blocks;   /* blocks of the rebin kernel, 0 = all that fit */
-  uint32_t reserved[6];
+  uint32_t solve_block;    /* threads per block of the solve kernels, a
+                              multiple of 32 up to 512, 0 = 256 */
+  uint32_t reserved[5];
 } WrachConfig;
 
 typedef struct WrachContext WrachContext;
@@ -159,6 +161,14 @@ int wrach_read(WrachContext *ctx, uint32_t world, float *positions,
 int wrach_tick(WrachContext *ctx, uint32_t world, float *positions,
                float *velocities, uint32_t *indices, uint32_t capacity);
 
+/* The draw pass (assets/shaders/draw.wgsl:18-40, MSAA 4 from
+ * runners/bevy/src/render/pipeline.rs:52-56) without a graphics API: each
+ * particle of the world's frame as a white square of half-size 0.4 world
+ * units on black, 4 samples per pixel, into `image` (height_px rows of
+ * width_px bytes, row 0 at the top, y up in the world).  Blocks. */
+int wrach_render(WrachContext *ctx, uint32_t world, uint32_t width_px,
+                 uint32_t height_px, uint8_t *image);
+
 /* Settings of a world (the uniform, with particles_in_frame_count). */
 int wrach_get_settings(WrachContext *ctx, uint32_t world,
                        WrachWorldSettings *out);
@@ -199,6 +209,64 @@ int wrach_rebin_trace(WrachContext *ctx, uint64_t *ns, uint32_t cap,
 
 /* The last error message of the context ("" if none). */
 const char *wrach_last_error(WrachContext *ctx);
+
+/* --- The learned solver surrogate (no counterpart in the reference) -------
+ * A per-particle MLP (64 -> 64 -> 64 -> 2, GELU, BF16 weights on the tensor
+ * cores, FP32 accumulation) reads each particle's 12 nearest neighbours'
+ * relative positions and velocities plus its own velocity and predicts the
+ * position correction of the first iterations-1 Jacobi iterations of the
+ * extended solve.  A surrogate frame applies that correction, runs the last
+ * plain iteration (with integration, walls and clamp) and falls back to the
+ * plain solve when the frame's mean penetration or kinetic-energy drift
+ * exceeds the given bounds.  Extended mode with iterations >= 2 only. */
+typedef struct WrachSurrogateStats {
+  uint32_t frames;
+  uint32_t fallbacks;
+  float mean_penetration;  /* mean over frames of the mean deepest overlap */
+  float max_penetration;   /* deepest overlap seen (px) */
+  float max_energy_drift;  /* largest relative kinetic-energy deviation */
+  uint32_t reserved[11];
+} WrachSurrogateStats;
+
+/* Parameters: w1 [64][64], b1 [64], w2 [64][64], b2 [64], w3 [64][8],
+ * b3 [8] (FP32, row = input, column = output; outputs 2..7 are padding). */
+uint32_t wrach_surrogate_param_count(void);
+/* Allocates the network (seeded Glorot-uniform init) and room for
+ * max_samples training rows; clears collected samples. */
+int wrach_surrogate_init(WrachContext *ctx, uint32_t seed,
+                         uint32_t max_samples);
+int wrach_surrogate_get_params(WrachContext *ctx, float *params,
+                               uint32_t count);
+int wrach_surrogate_set_params(WrachContext *ctx, const float *params,
+                               uint32_t count);
+/* Features of the current frame (BF16 rows of 64) into a device buffer of
+ * at least particles_in_frame rows. */
+int wrach_surrogate_features(WrachContext *ctx, uint16_t *d_x, uint32_t rows);
+/* Network outputs (n float pairs) of n device feature rows. */
+int wrach_surrogate_forward(WrachContext *ctx, const uint16_t *d_x,
+                            uint32_t n, float *d_y);
+/* Gradients (host, param_count floats) and loss of 0.5 * mean over the n
+ * rows of the squared error against d_t (n float pairs). */
+int wrach_surrogate_gradients(WrachContext *ctx, const uint16_t *d_x,
+                              const float *d_t, uint32_t n, float *grad,
+                              float *loss);
+/* Appends the current frame's features and plain-solver targets to the
+ * training set (the frame does not advance); *total = rows collected. */
+int wrach_surrogate_collect(WrachContext *ctx, uint32_t *total);
+/* `steps` Adam steps on batches of `batch` collected rows; *loss = the last
+ * batch's loss. */
+int wrach_surrogate_train(WrachContext *ctx, uint32_t steps, uint32_t batch,
+                          float lr, float *loss);
+/* For the current frame (which does not advance): the mean squared error,
+ * over particles that take part in the solve, of the network's correction
+ * against the plain solver's first-iterations correction, and the same for
+ * a zero correction (the frame without the network). */
+int wrach_surrogate_evaluate(WrachContext *ctx, float *mse_network,
+                             float *mse_zero);
+/* nsteps surrogate frames with the plain fallback gate; blocks per frame. */
+int wrach_surrogate_step(WrachContext *ctx, uint32_t nsteps,
+                         float max_penetration, float max_energy_drift,
+                         WrachSurrogateStats *stats);
 
 /* Runs one frame eagerly with a CUDA event between its kernel launches and
  * writes each launch's duration in milliseconds to ms[0 .. *count - 1]

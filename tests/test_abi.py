@@ -83,3 +83,17 @@ def test_grid_width_division_constants():
         assert m < 2 ** 32
         for x in [0, 1, gx - 1, gx, gx + 1, 2 ** 31 - 1] + [rng.randrange(2 ** 31) for _ in range(50)]:
             assert (x * m) >> s == x // gx
+
+
+def test_rust_binding_mirrors_the_header():
+    # bindings/rust/src/lib.rs declares the same config fields in the same
+    # order as the header's WrachConfig (ctypes mirror), and only functions
+    # the header declares
+    import wrach_gb300._lib as L
+    src = open(os.path.join(ROOT, "bindings", "rust", "src", "lib.rs")).read()
+    block = src[src.index("pub struct WrachConfigC {"):]
+    block = block[:block.index("}")]
+    rust_fields = re.findall(r"pub (\w+):", block)
+    assert rust_fields == [f for f, _ in L.Config._fields_]
+    externs = set(re.findall(r"fn (wrach_\w+)\(", src))
+    assert externs and externs <= declared_symbols()

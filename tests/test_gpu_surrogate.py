@@ -1,0 +1,126 @@
+"""The learned surrogate on the GPU: features bit-exact against the oracle,
+network forward pass and gradients against the CPU restatement
+(oracle/mlp_oracle.py) within BF16 tolerance, training on plain-solver
+trajectories, the ablation against the frame without the network, and the
+plain fallback gate."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as M
+from tests.helpers import same_bits
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    return pytest.importorskip("torch")
+
+
+def _sim(W, dims, capacity, iterations=4):
+    cfg = W.WrachConfig(dimensions=dims, cell_size=1, mode=1, iterations=iterations, gravity=0.1,
+                        capacity=capacity)
+    return W.Simulation(cfg)
+
+
+def test_features_match_oracle(W):
+    torch = _torch()
+    rng = np.random.default_rng(0)
+    dims = (60.0, 40.0)
+    pos = rng.uniform((0, 0), dims, size=(1500, 2)).astype(np.float32)
+    pos[:120] = (20.0 + rng.uniform(-1.2, 1.2, (120, 2))).astype(np.float32)  # over-full cells
+    vel = rng.normal(0, 0.7, size=pos.shape).astype(np.float32)
+    with _sim(W, dims, 4000) as sim:
+        sim.add_particles(pos, vel)
+        sim.surrogate_init(0, 16)
+        p, v, table = sim.read_frame()
+        n = len(p)
+        x = torch.zeros((n, 64), dtype=torch.int16, device="cuda")
+        sim.surrogate_features(x.data_ptr(), n)
+        sim.sync()
+        got = x.cpu().numpy().view(np.uint16)
+        s = sim.settings()
+        want = M.bf16_bits(M.features(s.grid_dimensions[0], s.grid_dimensions[1], 9, table, p, v))
+        assert np.array_equal(got, want.astype(np.uint16))
+
+
+def _random_net(rng, scale=0.25):
+    p = rng.normal(0, scale, M.N_PARAMS).astype(np.float32)
+    w1, b1, w2, b2, w3, b3 = M.unpack(p)
+    w3[:, 2:] = 0.0
+    b3[2:] = 0.0
+    return M.pack(w1, b1, w2, b2, w3, b3)
+
+
+def test_forward_and_gradients_match_oracle(W):
+    torch = _torch()
+    rng = np.random.default_rng(1)
+    with _sim(W, (30.0, 30.0), 100) as sim:
+        sim.surrogate_init(0, 16)
+        params = _random_net(rng)
+        sim.surrogate_set_params(params)
+        assert np.array_equal(sim.surrogate_params(), params)
+        n = 333
+        x = M.bf16(rng.normal(0, 0.7, (n, 64)).astype(np.float32))
+        t = rng.normal(0, 0.3, (n, 2)).astype(np.float32)
+        dx = torch.from_numpy((M.bf16_bits(x).astype(np.uint16)).view(np.int16)).cuda()
+        dt = torch.from_numpy(t).cuda()
+        dy = torch.zeros((n, 2), dtype=torch.float32, device="cuda")
+        sim.surrogate_forward(dx.data_ptr(), n, dy.data_ptr())
+        sim.sync()
+        y_gpu = dy.cpu().numpy()
+        y_cpu, _ = M.forward(params, x)
+        # BF16 activations: an FP32 vs float64 accumulation can flip an
+        # activation's BF16 rounding, one BF16 ulp (2^-8 relative)
+        assert np.abs(y_gpu - y_cpu).max() <= 2e-2 * np.abs(y_cpu).max()
+        g_gpu, l_gpu = sim.surrogate_gradients(dx.data_ptr(), dt.data_ptr(), n)
+        g_cpu, l_cpu = M.gradients(params, x, t)
+        assert abs(l_gpu - l_cpu) <= 1e-2 * l_cpu
+        for name, a, b in zip(("w1", "b1", "w2", "b2", "w3", "b3"), M.unpack(g_gpu), M.unpack(g_cpu)):
+            err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+            assert err < 3e-2, (name, err)
+
+
+def test_training_beats_the_frame_without_the_network(W):
+    # the ablation: trained on plain-solver frames, the network's correction
+    # is closer to the plain solver's first three iterations than the zero
+    # correction of the frame without it
+    from wrach_gb300 import workloads
+    dims, pos, vel = workloads.lattice(n=15000, width=240.0, height=136.0, sites=(167, 95))
+    with _sim(W, dims, 40000) as sim:
+        sim.add_particles(pos, vel)
+        sim.surrogate_init(0, 15000 * 40)
+        for _ in range(40):
+            sim.surrogate_collect()
+            sim.step(1)
+        first = sim.surrogate_train(1, 4096, 2e-3)
+        last = sim.surrogate_train(600, 4096, 2e-3)
+        assert last < first
+        ratios = []
+        for _ in range(5):
+            net, zero = sim.surrogate_evaluate()
+            ratios.append(net / zero)
+            sim.step(1)
+        print("held-out frames: mse(network) / mse(no network) =", np.round(ratios, 3))
+        assert np.mean(ratios) < 0.7
+
+
+def test_fallback_gate(W):
+    from wrach_gb300 import workloads
+    dims, pos, vel = workloads.lattice(n=12000, width=200.0, height=120.0, sites=(139, 87))
+    with _sim(W, dims, 30000) as sur, _sim(W, dims, 30000) as plain:
+        sur.add_particles(pos, vel)
+        plain.add_particles(pos, vel)
+        sur.surrogate_init(3, 16)
+        # a bound nothing can meet: every frame falls back to the plain solve,
+        # which must then equal plain frames bit for bit
+        st = sur.surrogate_step(6, max_penetration=-1.0, max_energy_drift=1e9)
+        plain.step(6)
+        assert st["frames"] == 6 and st["fallbacks"] == 6
+        a, b = sur.read_frame(), plain.read_frame()
+        assert np.array_equal(a[2], b[2]) and same_bits(a[0], b[0]) and same_bits(a[1], b[1])
+        # a bound nothing exceeds: no fallback, and a consistent frame
+        st = sur.surrogate_step(6, max_penetration=1e9, max_energy_drift=1e9)
+        assert st["frames"] == 6 and st["fallbacks"] == 0
+        p, v, t = sur.read_frame()
+        assert int(t[-1]) == len(pos) and np.all(np.diff(t.astype(np.int64)) >= 0)
+        assert st["max_energy_drift"] < 0.01

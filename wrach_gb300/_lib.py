@@ -64,7 +64,8 @@ class Config(ctypes.Structure):
                 ("capacity", ctypes.c_uint32),
                 ("device", ctypes.c_int32),
                 ("rebin_blocks", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 6)]
+                ("solve_block", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 5)]
 
 
 class Stats(ctypes.Structure):
@@ -72,6 +73,12 @@ class Stats(ctypes.Structure):
                 ("overflow", ctypes.c_uint32), ("rebin_blocks", ctypes.c_uint32),
                 ("tiles", ctypes.c_uint32), ("particles", ctypes.c_uint32),
                 ("cells", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 9)]
+
+
+class SurrogateStats(ctypes.Structure):
+    _fields_ = [("frames", ctypes.c_uint32), ("fallbacks", ctypes.c_uint32),
+                ("mean_penetration", ctypes.c_float), ("max_penetration", ctypes.c_float),
+                ("max_energy_drift", ctypes.c_float), ("reserved", ctypes.c_uint32 * 11)]
 
 
 # name -> (restype, argtypes); every symbol include/wrach.h declares
@@ -93,6 +100,8 @@ SIGNATURES = {
     "wrach_step": (ctypes.c_int, [_P, ctypes.c_uint32]),
     "wrach_read": (ctypes.c_int, [_P, ctypes.c_uint32, _F, _F, _U, ctypes.c_uint32]),
     "wrach_tick": (ctypes.c_int, [_P, ctypes.c_uint32, _F, _F, _U, ctypes.c_uint32]),
+    "wrach_render": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.POINTER(ctypes.c_uint8)]),
     "wrach_get_settings": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.POINTER(WorldSettings)]),
     "wrach_max_particles_per_frame": (ctypes.c_uint32, [ctypes.c_uint32, ctypes.c_uint32]),
     "wrach_capacity": (ctypes.c_uint32, [_P, ctypes.c_uint32]),
@@ -104,6 +113,18 @@ SIGNATURES = {
     "wrach_last_error": (ctypes.c_char_p, [_P]),
     "wrach_kernel_launches": (ctypes.c_uint64, [_P]),
     "wrach_stream": (ctypes.c_void_p, [_P]),
+    "wrach_surrogate_param_count": (ctypes.c_uint32, []),
+    "wrach_surrogate_init": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32]),
+    "wrach_surrogate_get_params": (ctypes.c_int, [_P, _F, ctypes.c_uint32]),
+    "wrach_surrogate_set_params": (ctypes.c_int, [_P, _F, ctypes.c_uint32]),
+    "wrach_surrogate_features": (ctypes.c_int, [_P, _P, ctypes.c_uint32]),
+    "wrach_surrogate_forward": (ctypes.c_int, [_P, _P, ctypes.c_uint32, _P]),
+    "wrach_surrogate_gradients": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _F, _F]),
+    "wrach_surrogate_collect": (ctypes.c_int, [_P, _U]),
+    "wrach_surrogate_evaluate": (ctypes.c_int, [_P, _F, _F]),
+    "wrach_surrogate_train": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _F]),
+    "wrach_surrogate_step": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                            ctypes.POINTER(SurrogateStats)]),
 }
 
 _lib = None

@@ -50,6 +50,7 @@ class WrachConfig:
     anchor: Tuple[float, float] = (0.0, 0.0)
     device: int = 0
     rebin_blocks: int = 0
+    solve_block: int = 0
 
     def to_c(self):
         c = _lib.Config()
@@ -66,6 +67,7 @@ class WrachConfig:
         c.capacity = int(self.capacity)
         c.device = int(self.device)
         c.rebin_blocks = int(self.rebin_blocks)
+        c.solve_block = int(self.solve_block)
         return c
 
 
@@ -186,6 +188,14 @@ class Simulation:
         n = int(idx[-1])
         return pos[:n], vel[:n], idx
 
+    def render(self, width_px, height_px, world=0):
+        """The frame drawn as the reference's draw pass does: an 8-bit image
+        (height_px, width_px), row 0 at the top."""
+        img = np.empty((int(height_px), int(width_px)), np.uint8)
+        self._check(self._L.wrach_render(self._ctx, world, int(width_px), int(height_px),
+                                         img.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        return img
+
     def sync(self):
         self._check(self._L.wrach_sync(self._ctx))
 
@@ -206,6 +216,59 @@ class Simulation:
         self._check(self._L.wrach_rebin_trace(self._ctx, buf, 32, ctypes.byref(cnt)))
         t = [int(buf[i]) for i in range(cnt.value)]
         return [b - a for a, b in zip(t, t[1:])]
+
+    # -- the learned surrogate ------------------------------------------------
+    def surrogate_init(self, seed=0, max_samples=1 << 20):
+        self._check(self._L.wrach_surrogate_init(self._ctx, int(seed), int(max_samples)))
+
+    def surrogate_params(self):
+        n = int(self._L.wrach_surrogate_param_count())
+        out = np.empty(n, np.float32)
+        self._check(self._L.wrach_surrogate_get_params(self._ctx, _f32p(out), n))
+        return out
+
+    def surrogate_set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        self._check(self._L.wrach_surrogate_set_params(self._ctx, _f32p(p), p.size))
+
+    def surrogate_features(self, d_x, rows):
+        self._check(self._L.wrach_surrogate_features(self._ctx, ctypes.c_void_p(d_x), int(rows)))
+
+    def surrogate_forward(self, d_x, n, d_y):
+        self._check(self._L.wrach_surrogate_forward(self._ctx, ctypes.c_void_p(d_x), int(n),
+                                                    ctypes.c_void_p(d_y)))
+
+    def surrogate_gradients(self, d_x, d_t, n):
+        g = np.empty(int(self._L.wrach_surrogate_param_count()), np.float32)
+        loss = ctypes.c_float(0)
+        self._check(self._L.wrach_surrogate_gradients(self._ctx, ctypes.c_void_p(d_x),
+                                                      ctypes.c_void_p(d_t), int(n), _f32p(g),
+                                                      ctypes.byref(loss)))
+        return g, float(loss.value)
+
+    def surrogate_collect(self):
+        total = ctypes.c_uint32(0)
+        self._check(self._L.wrach_surrogate_collect(self._ctx, ctypes.byref(total)))
+        return int(total.value)
+
+    def surrogate_evaluate(self):
+        """(mse of the network's correction, mse of a zero correction) on the
+        current frame against the plain solver's first-iterations correction."""
+        a, b = ctypes.c_float(0), ctypes.c_float(0)
+        self._check(self._L.wrach_surrogate_evaluate(self._ctx, ctypes.byref(a), ctypes.byref(b)))
+        return float(a.value), float(b.value)
+
+    def surrogate_train(self, steps, batch=4096, lr=1e-3):
+        loss = ctypes.c_float(0)
+        self._check(self._L.wrach_surrogate_train(self._ctx, int(steps), int(batch), float(lr),
+                                                  ctypes.byref(loss)))
+        return float(loss.value)
+
+    def surrogate_step(self, nsteps=1, max_penetration=0.2, max_energy_drift=0.01):
+        st = _lib.SurrogateStats()
+        self._check(self._L.wrach_surrogate_step(self._ctx, int(nsteps), float(max_penetration),
+                                                 float(max_energy_drift), ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in _lib.SurrogateStats._fields_ if f != "reserved"}
 
     @property
     def kernel_launches(self):

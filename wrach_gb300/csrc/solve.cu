@@ -35,7 +35,7 @@ __device__ __forceinline__ void publish_flags(Ctrl* ctrl, uint32_t flags) {
 //  - Particles::finish: integrate, boundaries, clamp, write (particles.rs:
 //    96-107, particle.rs:40-106)
 //  - handle_overflown_particles: the rest only integrate (cell.rs:79-95)
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
                   PhysDev ph, uint32_t ncells,
                   const uint32_t* __restrict__ cell_start,
@@ -94,7 +94,7 @@ k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
 // deterministic.  FINAL fuses gravity, integration, boundaries, the velocity
 // clamp and the key emission.
 template <bool FINAL>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
          uint32_t n, int do_push, const uint32_t* __restrict__ cell_start,
          const uint32_t* __restrict__ cell_of, const float2* __restrict__ qin,
@@ -192,7 +192,7 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
 
 cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st) {
   if (a.ncells == 0) return cudaSuccess;
-  const uint32_t threads = 256;
+  const uint32_t threads = a.block ? a.block : 256;
   const uint32_t blocks = (a.ncells + threads - 1) / threads;
   k_solve_reference<<<blocks, threads, 0, st>>>(
       a.worlds, a.nworlds, a.ph, a.ncells, a.cell_start, a.pos, a.vel,
@@ -204,7 +204,7 @@ cudaError_t launch_solve_extended(const SolveArgs& a, const float2* qin,
                                   float2* qout, bool final_pass, int do_push,
                                   cudaStream_t st) {
   if (a.n == 0) return cudaSuccess;
-  const uint32_t threads = 256;
+  const uint32_t threads = a.block ? a.block : 256;
   const uint32_t blocks = (a.n + threads - 1) / threads;
   if (final_pass)
     k_jacobi<true><<<blocks, threads, 0, st>>>(

@@ -1,0 +1,744 @@
+// The learned solver surrogate: a per-particle MLP that predicts the
+// position correction of the first K-1 Jacobi iterations of the extended
+// solve from the particle's k nearest neighbours.
+//
+//   features  k_knn_features: the 12 nearest taking-part particles within the
+//             5x5 cells around the particle (squared distance, ties by index),
+//             each as (dx, dy, dvx, dvy) relative to the particle, then the
+//             particle's own velocity; 50 values padded to 64, BF16.
+//   network   64 -> 64 -> 64 -> 2 (padded to 8), GELU (erf form) after the
+//             two hidden layers; BF16 weights, FP32 accumulation, on the
+//             tensor cores with mma.sync m16n8k16 (one warp per 16 rows; the
+//             accumulator fragment of one layer is the A fragment of the
+//             next, so the layers chain in registers).
+//   training  k_mlp_backward recomputes the forward pass of its rows and
+//             accumulates the gradients of 0.5 * mean squared error into
+//             FP32 buffers; k_adam updates FP32 master weights and refreshes
+//             their BF16 copies.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "wrach_internal.cuh"
+#include "wrach_kernels.h"
+
+namespace wrach {
+
+namespace {
+
+constexpr uint32_t kIn = kMlpIn, kHid = kMlpHidden, kOutPad = kMlpOutPad;
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, "
+      "{%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float gelu(float x) {
+  return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+}
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+// Shared-memory copy of the network: weights as BF16 in two layouts (WT
+// [out][in] for the forward pass, W [in][out] for the backward pass) and the
+// biases in FP32.
+struct SmemNet {
+  uint32_t w1t[kHid * kIn / 2], w2t[kHid * kHid / 2], w3t[kOutPad * kHid / 2];
+  uint32_t w1[kIn * kHid / 2], w2[kHid * kHid / 2], w3[kHid * kOutPad / 2];
+  float b1[kHid], b2[kHid], b3[kOutPad];
+};
+
+__device__ void load_net(const MlpDev& m, SmemNet& s, bool backward) {
+  const uint32_t* src;
+  for (uint32_t i = threadIdx.x; i < kHid * kIn / 2; i += blockDim.x) {
+    s.w1t[i] = reinterpret_cast<const uint32_t*>(m.w1t)[i];
+    s.w2t[i] = reinterpret_cast<const uint32_t*>(m.w2t)[i];
+    if (backward) {
+      s.w1[i] = reinterpret_cast<const uint32_t*>(m.w1)[i];
+      s.w2[i] = reinterpret_cast<const uint32_t*>(m.w2)[i];
+    }
+  }
+  src = reinterpret_cast<const uint32_t*>(m.w3t);
+  for (uint32_t i = threadIdx.x; i < kOutPad * kHid / 2; i += blockDim.x) {
+    s.w3t[i] = src[i];
+    if (backward) s.w3[i] = reinterpret_cast<const uint32_t*>(m.w3)[i];
+  }
+  for (uint32_t i = threadIdx.x; i < kHid; i += blockDim.x) {
+    s.b1[i] = m.b1[i];
+    s.b2[i] = m.b2[i];
+  }
+  for (uint32_t i = threadIdx.x; i < kOutPad; i += blockDim.x) s.b3[i] = m.b3[i];
+  __syncthreads();
+}
+
+// B fragment of W^T stored [n][k] (k contiguous, `kdim` columns): k-tile kk,
+// n-tile nt.
+__device__ __forceinline__ void bfrag(const uint32_t* wt, uint32_t kdim, uint32_t kk,
+                                      uint32_t nt, uint32_t lane, uint32_t& b0,
+                                      uint32_t& b1) {
+  const uint32_t g = lane >> 2, t = lane & 3;
+  const uint32_t row = (nt * 8 + g) * (kdim / 2);
+  b0 = wt[row + kk * 8 + t];
+  b1 = wt[row + kk * 8 + 4 + t];
+}
+
+// Forward pass of one 16-row tile held by a warp.  `ax` is the A fragment of
+// the input (4 k-tiles).  Writes the pre-activations z1, z2 (C layout, 8
+// n-tiles), the A fragments h1, h2 of the activations and the output y
+// (one n-tile).
+__device__ __forceinline__ void mlp_tile_forward(const SmemNet& s, uint32_t lane,
+                                                 const uint32_t (&ax)[4][4],
+                                                 float (&z1)[8][4], uint32_t (&h1)[4][4],
+                                                 float (&z2)[8][4], uint32_t (&h2)[4][4],
+                                                 float (&y)[4]) {
+  const uint32_t t = lane & 3;
+#pragma unroll
+  for (uint32_t nt = 0; nt < 8; ++nt) {
+    const float bl = s.b1[nt * 8 + 2 * t], bh = s.b1[nt * 8 + 2 * t + 1];
+    z1[nt][0] = bl; z1[nt][1] = bh; z1[nt][2] = bl; z1[nt][3] = bh;
+#pragma unroll
+    for (uint32_t kk = 0; kk < 4; ++kk) {
+      uint32_t b0, b1;
+      bfrag(s.w1t, kIn, kk, nt, lane, b0, b1);
+      mma_bf16(z1[nt], ax[kk], b0, b1);
+    }
+  }
+#pragma unroll
+  for (uint32_t kk = 0; kk < 4; ++kk) {
+    h1[kk][0] = pack_bf16(gelu(z1[2 * kk][0]), gelu(z1[2 * kk][1]));
+    h1[kk][1] = pack_bf16(gelu(z1[2 * kk][2]), gelu(z1[2 * kk][3]));
+    h1[kk][2] = pack_bf16(gelu(z1[2 * kk + 1][0]), gelu(z1[2 * kk + 1][1]));
+    h1[kk][3] = pack_bf16(gelu(z1[2 * kk + 1][2]), gelu(z1[2 * kk + 1][3]));
+  }
+#pragma unroll
+  for (uint32_t nt = 0; nt < 8; ++nt) {
+    const float bl = s.b2[nt * 8 + 2 * t], bh = s.b2[nt * 8 + 2 * t + 1];
+    z2[nt][0] = bl; z2[nt][1] = bh; z2[nt][2] = bl; z2[nt][3] = bh;
+#pragma unroll
+    for (uint32_t kk = 0; kk < 4; ++kk) {
+      uint32_t b0, b1;
+      bfrag(s.w2t, kHid, kk, nt, lane, b0, b1);
+      mma_bf16(z2[nt], h1[kk], b0, b1);
+    }
+  }
+#pragma unroll
+  for (uint32_t kk = 0; kk < 4; ++kk) {
+    h2[kk][0] = pack_bf16(gelu(z2[2 * kk][0]), gelu(z2[2 * kk][1]));
+    h2[kk][1] = pack_bf16(gelu(z2[2 * kk][2]), gelu(z2[2 * kk][3]));
+    h2[kk][2] = pack_bf16(gelu(z2[2 * kk + 1][0]), gelu(z2[2 * kk + 1][1]));
+    h2[kk][3] = pack_bf16(gelu(z2[2 * kk + 1][2]), gelu(z2[2 * kk + 1][3]));
+  }
+  {
+    const float bl = s.b3[2 * t], bh = s.b3[2 * t + 1];
+    y[0] = bl; y[1] = bh; y[2] = bl; y[3] = bh;
+#pragma unroll
+    for (uint32_t kk = 0; kk < 4; ++kk) {
+      uint32_t b0, b1;
+      bfrag(s.w3t, kHid, kk, 0, lane, b0, b1);
+      mma_bf16(y, h2[kk], b0, b1);
+    }
+  }
+}
+
+// A fragment (4 k-tiles) of 16 rows of X (BF16 [rows][64]); rows past n read
+// as zero.
+__device__ __forceinline__ void load_x_tile(const uint16_t* x, uint32_t row0, uint32_t n,
+                                            uint32_t lane, uint32_t (&ax)[4][4]) {
+  const uint32_t g = lane >> 2, t = lane & 3;
+  const uint32_t r0 = row0 + g, r1 = row0 + g + 8;
+  const uint32_t* p0 = reinterpret_cast<const uint32_t*>(x + (size_t)r0 * kIn);
+  const uint32_t* p1 = reinterpret_cast<const uint32_t*>(x + (size_t)r1 * kIn);
+#pragma unroll
+  for (uint32_t kk = 0; kk < 4; ++kk) {
+    ax[kk][0] = r0 < n ? p0[kk * 8 + t] : 0u;
+    ax[kk][1] = r1 < n ? p1[kk * 8 + t] : 0u;
+    ax[kk][2] = r0 < n ? p0[kk * 8 + 4 + t] : 0u;
+    ax[kk][3] = r1 < n ? p1[kk * 8 + 4 + t] : 0u;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_mlp_forward(MlpDev m, const uint16_t* __restrict__ x,
+                                                     uint32_t n, float2* __restrict__ y) {
+  __shared__ SmemNet s;
+  load_net(m, s, false);
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t g = lane >> 2, t = lane & 3;
+  const uint32_t tiles = (n + 15) / 16;
+  for (uint32_t tile = blockIdx.x * 4 + warp; tile < tiles; tile += gridDim.x * 4) {
+    uint32_t ax[4][4], h1[4][4], h2[4][4];
+    float z1[8][4], z2[8][4], out[4];
+    load_x_tile(x, tile * 16, n, lane, ax);
+    mlp_tile_forward(s, lane, ax, z1, h1, z2, h2, out);
+    if (t == 0) {
+      const uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
+      if (r0 < n) y[r0] = make_float2(out[0], out[1]);
+      if (r1 < n) y[r1] = make_float2(out[2], out[3]);
+    }
+  }
+}
+
+// Per-warp scratch of the backward pass: activations and gradients of one
+// tile stored transposed ([feature][row], rows contiguous) as BF16 pairs, the
+// A operand layout of the weight-gradient products X^T dZ1, H1^T dZ2, H2^T dY.
+struct SmemBack {
+  uint16_t xt[kIn][16], h1t[kHid][16], h2t[kHid][16];
+  uint16_t dz1t[kHid][16], dz2t[kHid][16], dyt[kOutPad][16];
+};
+
+// Accumulators of the block: FP32 gradients, in the parameter order.
+struct SmemGrad {
+  float w1[kIn * kHid], b1[kHid], w2[kHid * kHid], b2[kHid], w3[kHid * kOutPad], b3[kOutPad];
+};
+static_assert(sizeof(SmemGrad) == kMlpParams * sizeof(float), "gradient order = parameters");
+
+__device__ __forceinline__ uint16_t bf16_bits(float v) {
+  __nv_bfloat16 b = __float2bfloat16_rn(v);
+  return *reinterpret_cast<uint16_t*>(&b);
+}
+
+// Scatter a C-layout tile (8 n-tiles of 16x8) into a transposed BF16 array.
+__device__ __forceinline__ void store_ct(uint16_t (*dst)[16], const float (&c)[8][4],
+                                         uint32_t lane) {
+  const uint32_t g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (uint32_t nt = 0; nt < 8; ++nt) {
+    const uint32_t col = nt * 8 + 2 * t;
+    dst[col][g] = bf16_bits(c[nt][0]);
+    dst[col + 1][g] = bf16_bits(c[nt][1]);
+    dst[col][g + 8] = bf16_bits(c[nt][2]);
+    dst[col + 1][g + 8] = bf16_bits(c[nt][3]);
+  }
+}
+
+// Scatter an A-layout BF16 tile (4 k-tiles) into a transposed array.
+__device__ __forceinline__ void store_at(uint16_t (*dst)[16], const uint32_t (&a)[4][4],
+                                         uint32_t lane) {
+  const uint32_t g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (uint32_t kk = 0; kk < 4; ++kk) {
+    const uint32_t c0 = kk * 16 + 2 * t, c1 = c0 + 8;
+    dst[c0][g] = (uint16_t)(a[kk][0] & 0xFFFF);
+    dst[c0 + 1][g] = (uint16_t)(a[kk][0] >> 16);
+    dst[c0][g + 8] = (uint16_t)(a[kk][1] & 0xFFFF);
+    dst[c0 + 1][g + 8] = (uint16_t)(a[kk][1] >> 16);
+    dst[c1][g] = (uint16_t)(a[kk][2] & 0xFFFF);
+    dst[c1 + 1][g] = (uint16_t)(a[kk][2] >> 16);
+    dst[c1][g + 8] = (uint16_t)(a[kk][3] & 0xFFFF);
+    dst[c1 + 1][g + 8] = (uint16_t)(a[kk][3] >> 16);
+  }
+}
+
+// dW[m][n] += sum over the 16 rows of AT[m][row] * BT[n][row] for m in
+// [0, mdim), n in [0, ndim): the tile's weight-gradient product on the
+// tensor cores (K = 16 rows), added into the block's FP32 accumulator.
+__device__ __forceinline__ void grad_product(const uint16_t (*at)[16], uint32_t mdim,
+                                             const uint16_t (*bt)[16], uint32_t ndim,
+                                             float* acc, uint32_t lane) {
+  const uint32_t g = lane >> 2, t = lane & 3;
+  for (uint32_t mt = 0; mt < mdim / 16; ++mt) {
+    uint32_t a[4];
+    a[0] = *reinterpret_cast<const uint32_t*>(&at[mt * 16 + g][2 * t]);
+    a[1] = *reinterpret_cast<const uint32_t*>(&at[mt * 16 + g + 8][2 * t]);
+    a[2] = *reinterpret_cast<const uint32_t*>(&at[mt * 16 + g][2 * t + 8]);
+    a[3] = *reinterpret_cast<const uint32_t*>(&at[mt * 16 + g + 8][2 * t + 8]);
+    for (uint32_t nt = 0; nt < ndim / 8; ++nt) {
+      const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&bt[nt * 8 + g][2 * t]);
+      const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&bt[nt * 8 + g][2 * t + 8]);
+      float d[4] = {0.f, 0.f, 0.f, 0.f};
+      mma_bf16(d, a, b0, b1);
+      const uint32_t m0 = mt * 16 + g, n0 = nt * 8 + 2 * t;
+      atomicAdd(&acc[m0 * ndim + n0], d[0]);
+      atomicAdd(&acc[m0 * ndim + n0 + 1], d[1]);
+      atomicAdd(&acc[(m0 + 8) * ndim + n0], d[2]);
+      atomicAdd(&acc[(m0 + 8) * ndim + n0 + 1], d[3]);
+    }
+  }
+}
+
+// Gradients of L = 0.5 * sum over rows and the 2 outputs of (y - target)^2 /
+// `scale_rows` with respect to every parameter, added into `grad` (FP32,
+// the MlpDev parameter order: w1 [in][out], b1, w2, b2, w3 [in][8], b3).
+// Also adds the loss into *loss.
+__global__ void __launch_bounds__(128) k_mlp_backward(MlpDev m, const uint16_t* __restrict__ x,
+                                                      const float2* __restrict__ target,
+                                                      uint32_t n, float inv_rows,
+                                                      float* __restrict__ grad,
+                                                      float* __restrict__ loss) {
+  extern __shared__ __align__(16) uint8_t dyn[];
+  SmemNet& s = *reinterpret_cast<SmemNet*>(dyn);
+  SmemGrad& acc = *reinterpret_cast<SmemGrad*>(dyn + sizeof(SmemNet));
+  SmemBack* back = reinterpret_cast<SmemBack*>(dyn + sizeof(SmemNet) + sizeof(SmemGrad));
+  load_net(m, s, true);
+  float* accf = reinterpret_cast<float*>(&acc);
+  for (uint32_t i = threadIdx.x; i < sizeof(SmemGrad) / 4; i += blockDim.x) accf[i] = 0.f;
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t g = lane >> 2, t = lane & 3;
+  SmemBack& sb = back[warp];
+  float lsum = 0.f;
+  const uint32_t tiles = (n + 15) / 16;
+  for (uint32_t tile = blockIdx.x * 4 + warp; tile < tiles; tile += gridDim.x * 4) {
+    uint32_t ax[4][4], h1[4][4], h2[4][4];
+    float z1[8][4], z2[8][4], y[4];
+    load_x_tile(x, tile * 16, n, lane, ax);
+    mlp_tile_forward(s, lane, ax, z1, h1, z2, h2, y);
+    // dY (C layout, one n-tile; only columns 0 and 1 are real outputs)
+    const uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
+    float dy[4] = {0.f, 0.f, 0.f, 0.f};
+    if (t == 0) {
+      if (r0 < n) {
+        const float2 tg = target[r0];
+        const float e0 = y[0] - tg.x, e1 = y[1] - tg.y;
+        lsum += 0.5f * (e0 * e0 + e1 * e1);
+        dy[0] = e0 * inv_rows;
+        dy[1] = e1 * inv_rows;
+      }
+      if (r1 < n) {
+        const float2 tg = target[r1];
+        const float e0 = y[2] - tg.x, e1 = y[3] - tg.y;
+        lsum += 0.5f * (e0 * e0 + e1 * e1);
+        dy[2] = e0 * inv_rows;
+        dy[3] = e1 * inv_rows;
+      }
+    }
+    // dH2 = dY W3^T  (K = 8 outputs padded to 16 with zeros)
+    uint32_t ady[4];
+    ady[0] = pack_bf16(dy[0], dy[1]);
+    ady[1] = pack_bf16(dy[2], dy[3]);
+    ady[2] = 0u;
+    ady[3] = 0u;
+    float dz2[8][4];
+#pragma unroll
+    for (uint32_t nt = 0; nt < 8; ++nt) {
+      dz2[nt][0] = dz2[nt][1] = dz2[nt][2] = dz2[nt][3] = 0.f;
+      // B(k = out, n = in) = W3[in][out]; W3 stored [in][8]
+      const uint32_t b0 = s.w3[(nt * 8 + g) * (kOutPad / 2) + t];
+      mma_bf16(dz2[nt], ady, b0, 0u);
+    }
+#pragma unroll
+    for (uint32_t nt = 0; nt < 8; ++nt)
+#pragma unroll
+      for (uint32_t q = 0; q < 4; ++q) dz2[nt][q] *= gelu_grad(z2[nt][q]);
+    // dH1 = dZ2 W2^T
+    uint32_t adz2[4][4];
+#pragma unroll
+    for (uint32_t kk = 0; kk < 4; ++kk) {
+      adz2[kk][0] = pack_bf16(dz2[2 * kk][0], dz2[2 * kk][1]);
+      adz2[kk][1] = pack_bf16(dz2[2 * kk][2], dz2[2 * kk][3]);
+      adz2[kk][2] = pack_bf16(dz2[2 * kk + 1][0], dz2[2 * kk + 1][1]);
+      adz2[kk][3] = pack_bf16(dz2[2 * kk + 1][2], dz2[2 * kk + 1][3]);
+    }
+    float dz1[8][4];
+#pragma unroll
+    for (uint32_t nt = 0; nt < 8; ++nt) {
+      dz1[nt][0] = dz1[nt][1] = dz1[nt][2] = dz1[nt][3] = 0.f;
+#pragma unroll
+      for (uint32_t kk = 0; kk < 4; ++kk) {
+        uint32_t b0, b1;
+        bfrag(s.w2, kHid, kk, nt, lane, b0, b1);  // W2 [in][out]: B(k=out, n=in)
+        mma_bf16(dz1[nt], adz2[kk], b0, b1);
+      }
+    }
+#pragma unroll
+    for (uint32_t nt = 0; nt < 8; ++nt)
+#pragma unroll
+      for (uint32_t q = 0; q < 4; ++q) dz1[nt][q] *= gelu_grad(z1[nt][q]);
+
+    // bias gradients: column sums over the tile's rows
+#pragma unroll
+    for (uint32_t nt = 0; nt < 8; ++nt) {
+      float s2a = dz2[nt][0] + dz2[nt][2], s2b = dz2[nt][1] + dz2[nt][3];
+      float s1a = dz1[nt][0] + dz1[nt][2], s1b = dz1[nt][1] + dz1[nt][3];
+#pragma unroll
+      for (uint32_t o = 4; o < 32; o <<= 1) {
+        s2a += __shfl_xor_sync(0xffffffffu, s2a, o);
+        s2b += __shfl_xor_sync(0xffffffffu, s2b, o);
+        s1a += __shfl_xor_sync(0xffffffffu, s1a, o);
+        s1b += __shfl_xor_sync(0xffffffffu, s1b, o);
+      }
+      if (g == 0) {
+        atomicAdd(&acc.b2[nt * 8 + 2 * t], s2a);
+        atomicAdd(&acc.b2[nt * 8 + 2 * t + 1], s2b);
+        atomicAdd(&acc.b1[nt * 8 + 2 * t], s1a);
+        atomicAdd(&acc.b1[nt * 8 + 2 * t + 1], s1b);
+      }
+    }
+    {
+      float a0 = dy[0] + dy[2], a1 = dy[1] + dy[3];
+#pragma unroll
+      for (uint32_t o = 4; o < 32; o <<= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      }
+      if (g == 0 && t == 0) {
+        atomicAdd(&acc.b3[0], a0);
+        atomicAdd(&acc.b3[1], a1);
+      }
+    }
+    // weight gradients: X^T dZ1, H1^T dZ2, H2^T dY (K = the tile's 16 rows)
+    store_at(sb.xt, ax, lane);
+    store_at(sb.h1t, h1, lane);
+    store_at(sb.h2t, h2, lane);
+    store_ct(sb.dz1t, dz1, lane);
+    store_ct(sb.dz2t, dz2, lane);
+    {
+      // dY transposed: 8 output columns x 16 rows
+      for (uint32_t c = 0; c < kOutPad; ++c) {
+        sb.dyt[c][g] = 0;
+        sb.dyt[c][g + 8] = 0;
+      }
+      __syncwarp();
+      if (t == 0) {
+        sb.dyt[0][g] = bf16_bits(dy[0]);
+        sb.dyt[1][g] = bf16_bits(dy[1]);
+        sb.dyt[0][g + 8] = bf16_bits(dy[2]);
+        sb.dyt[1][g + 8] = bf16_bits(dy[3]);
+      }
+    }
+    __syncwarp();
+    grad_product(sb.xt, kIn, sb.dz1t, kHid, acc.w1, lane);
+    grad_product(sb.h1t, kHid, sb.dz2t, kHid, acc.w2, lane);
+    grad_product(sb.h2t, kHid, sb.dyt, kOutPad, acc.w3, lane);
+    __syncwarp();
+  }
+  // the tile losses of the warp, then the block's gradients into global
+#pragma unroll
+  for (uint32_t o = 1; o < 32; o <<= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  if (lane == 0 && lsum != 0.f) atomicAdd(loss, lsum * inv_rows);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < sizeof(SmemGrad) / 4; i += blockDim.x)
+    if (accf[i] != 0.f) atomicAdd(&grad[i], accf[i]);
+}
+
+size_t backward_smem() {
+  return sizeof(SmemNet) + sizeof(SmemGrad) + 4 * sizeof(SmemBack);
+}
+
+// Adam on the FP32 master parameters (the SmemGrad order), then the BF16
+// copies in both layouts.
+__global__ void k_adam(MlpDev m, const float* __restrict__ grad, float* __restrict__ mom1,
+                       float* __restrict__ mom2, float lr, float b1, float b2, float eps,
+                       float bc1, float bc2, uint32_t nparams) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nparams) return;
+  const float gr = grad[i];
+  const float a = b1 * mom1[i] + (1.f - b1) * gr;
+  const float b = b2 * mom2[i] + (1.f - b2) * gr * gr;
+  mom1[i] = a;
+  mom2[i] = b;
+  const float step = lr * (a / bc1) / (sqrtf(b / bc2) + eps);
+  float* p = m.params;
+  const float v = p[i] - step;
+  p[i] = v;
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  // parameter order: w1 [in][hid], b1, w2 [hid][hid], b2, w3 [hid][8], b3
+  const uint32_t o_b1 = kIn * kHid, o_w2 = o_b1 + kHid, o_b2 = o_w2 + kHid * kHid;
+  const uint32_t o_w3 = o_b2 + kHid, o_b3 = o_w3 + kHid * kOutPad;
+  __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(m.w1);
+  __nv_bfloat16* w1t = reinterpret_cast<__nv_bfloat16*>(m.w1t);
+  __nv_bfloat16* w2 = reinterpret_cast<__nv_bfloat16*>(m.w2);
+  __nv_bfloat16* w2t = reinterpret_cast<__nv_bfloat16*>(m.w2t);
+  __nv_bfloat16* w3 = reinterpret_cast<__nv_bfloat16*>(m.w3);
+  __nv_bfloat16* w3t = reinterpret_cast<__nv_bfloat16*>(m.w3t);
+  if (i < o_b1) {
+    const uint32_t r = i / kHid, c = i % kHid;  // in, out
+    w1[i] = h;
+    w1t[c * kIn + r] = h;
+  } else if (i < o_w2) {
+    m.b1[i - o_b1] = v;
+  } else if (i < o_b2) {
+    const uint32_t j = i - o_w2, r = j / kHid, c = j % kHid;
+    w2[j] = h;
+    w2t[c * kHid + r] = h;
+  } else if (i < o_w3) {
+    m.b2[i - o_b2] = v;
+  } else if (i < o_b3) {
+    const uint32_t j = i - o_w3, r = j / kOutPad, c = j % kOutPad;
+    w3[j] = h;
+    w3t[c * kHid + r] = h;
+  } else {
+    m.b3[i - o_b3] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Features
+// ---------------------------------------------------------------------------
+
+constexpr uint32_t kK = kKnn;
+
+// Features of the binned state (one thread per particle): the 12 nearest
+// taking-part particles (the first `cap` of each cell) in the 5x5 cells
+// around the particle's cell, by squared distance, ties by index; each as
+// (dx, dy, dvx, dvy); then the own velocity; zero padding to 64.  Particles
+// that do not take part (past the capacity of their cell) get all zeros.
+__global__ void __launch_bounds__(256)
+k_knn_features(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32_t n,
+               const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ cell_of,
+               const float2* __restrict__ pos, const float2* __restrict__ vel,
+               uint16_t* __restrict__ x) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t* row = reinterpret_cast<uint32_t*>(x + (size_t)i * kIn);
+  const uint32_t c = cell_of[i];
+  if (i - cell_start[c] >= ph.cap) {
+    for (uint32_t k = 0; k < kIn / 2; ++k) row[k] = 0u;
+    return;
+  }
+  const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
+  uint32_t cx, cy;
+  cell_xy(w, c - w.cell_off, cx, cy);
+  const float2 pi = pos[i], vi = vel[i];
+  float bd[kK];
+  uint32_t bj[kK];
+#pragma unroll
+  for (uint32_t k = 0; k < kK; ++k) {
+    bd[k] = INFINITY;
+    bj[k] = 0xFFFFFFFFu;
+  }
+  const int y0 = max((int)cy - 2, 0), y1 = min((int)cy + 2, (int)w.gy - 1);
+  const int x0 = max((int)cx - 2, 0), x1 = min((int)cx + 2, (int)w.gx - 1);
+  for (int ny = y0; ny <= y1; ++ny) {
+    const uint32_t rb = w.cell_off + (uint32_t)ny * w.gx;
+    for (int nx = x0; nx <= x1; ++nx) {
+      const uint32_t js = cell_start[rb + nx];
+      const uint32_t je = min(cell_start[rb + nx + 1], js + ph.cap);
+      for (uint32_t j = js; j < je; ++j) {
+        if (j == i) continue;
+        const float2 pj = pos[j];
+        const float dx = pj.x - pi.x, dy = pj.y - pi.y;
+        float d = dx * dx + dy * dy;
+        if (!(d < bd[kK - 1]) && !(d == bd[kK - 1] && j < bj[kK - 1])) continue;
+        uint32_t jj = j;
+        // insert, keeping (distance, index) ascending
+#pragma unroll
+        for (uint32_t k = 0; k < kK; ++k) {
+          const bool less = d < bd[k] || (d == bd[k] && jj < bj[k]);
+          if (less) {
+            const float td = bd[k];
+            const uint32_t tj = bj[k];
+            bd[k] = d;
+            bj[k] = jj;
+            d = td;
+            jj = tj;
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (uint32_t k = 0; k < kK; ++k) {
+    if (bj[k] != 0xFFFFFFFFu) {
+      const float2 pj = pos[bj[k]], vj = vel[bj[k]];
+      row[2 * k] = pack_bf16(pj.x - pi.x, pj.y - pi.y);
+      row[2 * k + 1] = pack_bf16(vj.x - vi.x, vj.y - vi.y);
+    } else {
+      row[2 * k] = 0u;
+      row[2 * k + 1] = 0u;
+    }
+  }
+  row[2 * kK] = pack_bf16(vi.x, vi.y);
+  for (uint32_t k = 2 * kK + 1; k < kIn / 2; ++k) row[k] = 0u;
+}
+
+// q = p + the network's correction for taking-part particles; p otherwise.
+__global__ void k_apply_correction(const WorldDev* __restrict__ worlds, PhysDev ph, uint32_t n,
+                                   const uint32_t* __restrict__ cell_start,
+                                   const uint32_t* __restrict__ cell_of,
+                                   const float2* __restrict__ pos, const float2* __restrict__ corr,
+                                   float2* __restrict__ q) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float2 p = pos[i];
+  if (i - cell_start[cell_of[i]] >= ph.cap) {
+    q[i] = p;
+    return;
+  }
+  const float2 c = corr[i];
+  q[i] = make_float2(p.x + c.x, p.y + c.y);
+}
+
+// target = q - p (the first K-1 iterations' correction)
+__global__ void k_target(uint32_t n, const float2* __restrict__ pos, const float2* __restrict__ q,
+                         float2* __restrict__ target) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float2 p = pos[i], v = q[i];
+  target[i] = make_float2(v.x - p.x, v.y - p.y);
+}
+
+// Frame metrics of the gate: per taking-part particle the deepest overlap
+// with a neighbour of the 3x3 cells (min_d - distance, if positive), summed
+// and maxed; and the kinetic energy.  out[0] += sum of overlaps, out[1] =
+// max overlap (as float bits, non-negative so integer max works), out[2] +=
+// number of particles, out[3] += kinetic energy, out[4] += the kinetic
+// energy the plain frame would have.
+__global__ void __launch_bounds__(256)
+k_penetration(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32_t n,
+              const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ cell_of,
+              const float2* __restrict__ pos, const float2* __restrict__ vel,
+              const float2* __restrict__ vel_before, float* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  float pen = 0.f, ke = 0.f, cnt = 0.f, ke_plain = 0.f;
+  if (i < n) {
+    const float2 v = vel[i];
+    ke = 0.5f * (v.x * v.x + v.y * v.y);
+    // the plain frame's kinetic energy: its velocity changes only through
+    // gravity, the clamp and wall reflections (which keep |v|)
+    const float2 u = vel_before[i];
+    const float ux = fminf(fmaxf(u.x, -ph.vmax), ph.vmax);
+    const float uy = fminf(fmaxf(u.y - ph.gravity, -ph.vmax), ph.vmax);
+    ke_plain = 0.5f * (ux * ux + uy * uy);
+    const uint32_t c = cell_of[i];
+    if (i - cell_start[c] < ph.cap) {
+      cnt = 1.f;
+      const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
+      uint32_t cx, cy;
+      cell_xy(w, c - w.cell_off, cx, cy);
+      const float2 pi = pos[i];
+      const int y0 = max((int)cy - 1, 0), y1 = min((int)cy + 1, (int)w.gy - 1);
+      const int x0 = max((int)cx - 1, 0), x1 = min((int)cx + 1, (int)w.gx - 1);
+      for (int ny = y0; ny <= y1; ++ny) {
+        const uint32_t rb = w.cell_off + (uint32_t)ny * w.gx;
+        for (int nx = x0; nx <= x1; ++nx) {
+          const uint32_t js = cell_start[rb + nx];
+          const uint32_t je = min(cell_start[rb + nx + 1], js + ph.cap);
+          for (uint32_t j = js; j < je; ++j) {
+            if (j == i) continue;
+            const float2 pj = pos[j];
+            const float dx = pj.x - pi.x, dy = pj.y - pi.y;
+            const float d = sqrtf(dx * dx + dy * dy);
+            pen = fmaxf(pen, ph.min_d - d);
+          }
+        }
+      }
+    }
+  }
+  float s = pen, k = ke, m = pen, nc = cnt, kp = ke_plain;
+#pragma unroll
+  for (uint32_t o = 1; o < 32; o <<= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    k += __shfl_xor_sync(0xffffffffu, k, o);
+    kp += __shfl_xor_sync(0xffffffffu, kp, o);
+    nc += __shfl_xor_sync(0xffffffffu, nc, o);
+    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&out[0], s);
+    atomicMax(reinterpret_cast<int*>(&out[1]), __float_as_int(m));
+    atomicAdd(&out[2], nc);
+    atomicAdd(&out[3], k);
+    atomicAdd(&out[4], kp);
+  }
+}
+
+// Squared errors of the correction against the target, and of zero against
+// the target, over taking-part particles: out[0] += |corr - t|^2,
+// out[1] += |t|^2, out[2] += count.
+__global__ void k_errors(PhysDev ph, uint32_t n, const uint32_t* __restrict__ cell_start,
+                         const uint32_t* __restrict__ cell_of, const float2* __restrict__ corr,
+                         const float2* __restrict__ target, float* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  float e = 0.f, z = 0.f, c = 0.f;
+  if (i < n && i - cell_start[cell_of[i]] < ph.cap) {
+    const float2 a = corr[i], t = target[i];
+    e = (a.x - t.x) * (a.x - t.x) + (a.y - t.y) * (a.y - t.y);
+    z = t.x * t.x + t.y * t.y;
+    c = 1.f;
+  }
+#pragma unroll
+  for (uint32_t o = 1; o < 32; o <<= 1) {
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+    z += __shfl_xor_sync(0xffffffffu, z, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&out[0], e);
+    atomicAdd(&out[1], z);
+    atomicAdd(&out[2], c);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_errors(const SolveArgs& a, const float2* corr, const float2* target, float* out,
+                          cudaStream_t st) {
+  if (a.n == 0) return cudaSuccess;
+  k_errors<<<(a.n + 255) / 256, 256, 0, st>>>(a.ph, a.n, a.cell_start, a.cell_of, corr, target,
+                                              out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_knn_features(const SolveArgs& a, uint16_t* x, cudaStream_t st) {
+  if (a.n == 0) return cudaSuccess;
+  k_knn_features<<<(a.n + 255) / 256, 256, 0, st>>>(a.worlds, a.nworlds, a.ph, a.n,
+                                                    a.cell_start, a.cell_of, a.pos, a.vel, x);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_forward(const MlpDev& m, const uint16_t* x, uint32_t n, float2* y,
+                               int blocks, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const int need = (int)((n + 63) / 64);
+  k_mlp_forward<<<need < blocks ? need : blocks, 128, 0, st>>>(m, x, n, y);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_backward(const MlpDev& m, const uint16_t* x, const float2* target,
+                                uint32_t n, float inv_rows, float* grad, float* loss, int blocks,
+                                cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const size_t smem = backward_smem();
+  cudaError_t e = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  const int need = (int)((n + 63) / 64);
+  k_mlp_backward<<<need < blocks ? need : blocks, 128, smem, st>>>(m, x, target, n, inv_rows,
+                                                                   grad, loss);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adam(const MlpDev& m, const float* grad, float* mom1, float* mom2, float lr,
+                        uint32_t step, cudaStream_t st) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float bc1 = 1.f - powf(b1, (float)step), bc2 = 1.f - powf(b2, (float)step);
+  k_adam<<<(kMlpParams + 255) / 256, 256, 0, st>>>(m, grad, mom1, mom2, lr, b1, b2, eps, bc1,
+                                                    bc2, kMlpParams);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apply_correction(const SolveArgs& a, const float2* corr, float2* q,
+                                    cudaStream_t st) {
+  if (a.n == 0) return cudaSuccess;
+  k_apply_correction<<<(a.n + 255) / 256, 256, 0, st>>>(a.worlds, a.ph, a.n, a.cell_start,
+                                                        a.cell_of, a.pos, corr, q);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_target(uint32_t n, const float2* pos, const float2* q, float2* target,
+                          cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_target<<<(n + 255) / 256, 256, 0, st>>>(n, pos, q, target);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_penetration(const SolveArgs& a, const float2* pos, const float2* vel,
+                               float* out, cudaStream_t st) {
+  if (a.n == 0) return cudaSuccess;
+  k_penetration<<<(a.n + 255) / 256, 256, 0, st>>>(a.worlds, a.nworlds, a.ph, a.n, a.cell_start,
+                                                   a.cell_of, pos, vel, a.vel, out);
+  return cudaGetLastError();
+}
+
+}  // namespace wrach

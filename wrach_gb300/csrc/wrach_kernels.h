@@ -22,6 +22,7 @@ struct SolveArgs {
   float2* vel_out;
   uint32_t* keys;               // next cell of each output particle
   Ctrl* ctrl;
+  uint32_t block;               // threads per block of the solve kernels (<= 512)
 };
 
 cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st);
@@ -85,5 +86,51 @@ cudaError_t launch_upload_keys(const WorldDev* worlds, int nworlds,
 // cell-start table.
 cudaError_t launch_world_table(const uint32_t* cell_start, uint32_t cell_off,
                                uint32_t cells, uint32_t* out, cudaStream_t st);
+
+// The surrogate network (surrogate.cu): FP32 master parameters in the order
+// w1 [64 in][64 out], b1 [64], w2 [64][64], b2 [64], w3 [64][8], b3 [8]
+// (outputs 2..7 of the last layer are padding), and BF16 copies of the
+// weights in two layouts.
+constexpr uint32_t kMlpIn = 64, kMlpHidden = 64, kMlpOutPad = 8;
+constexpr uint32_t kMlpParams =
+    kMlpIn * kMlpHidden + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden +
+    kMlpHidden * kMlpOutPad + kMlpOutPad;
+constexpr uint32_t kKnn = 12;
+
+struct MlpDev {
+  float* params;           // kMlpParams
+  float* b1;               // into params
+  float* b2;
+  float* b3;
+  uint16_t* w1;            // BF16 [in][out]
+  uint16_t* w1t;           // BF16 [out][in]
+  uint16_t* w2;
+  uint16_t* w2t;
+  uint16_t* w3;            // BF16 [in][8]
+  uint16_t* w3t;           // BF16 [8][in]
+};
+
+cudaError_t launch_knn_features(const SolveArgs& a, uint16_t* x, cudaStream_t st);
+cudaError_t launch_mlp_forward(const MlpDev& m, const uint16_t* x, uint32_t n, float2* y,
+                               int blocks, cudaStream_t st);
+cudaError_t launch_mlp_backward(const MlpDev& m, const uint16_t* x, const float2* target,
+                                uint32_t n, float inv_rows, float* grad, float* loss,
+                                int blocks, cudaStream_t st);
+cudaError_t launch_adam(const MlpDev& m, const float* grad, float* mom1, float* mom2, float lr,
+                        uint32_t step, cudaStream_t st);
+cudaError_t launch_apply_correction(const SolveArgs& a, const float2* corr, float2* q,
+                                    cudaStream_t st);
+cudaError_t launch_target(uint32_t n, const float2* pos, const float2* q, float2* target,
+                          cudaStream_t st);
+cudaError_t launch_errors(const SolveArgs& a, const float2* corr, const float2* target, float* out,
+                          cudaStream_t st);
+cudaError_t launch_penetration(const SolveArgs& a, const float2* pos, const float2* vel,
+                               float* out, cudaStream_t st);
+
+// Headless point rasteriser (render.cu): `cover` holds width_px * height_px
+// u32 scratch, `image` the 8-bit result.
+cudaError_t launch_render(const float2* pos, uint32_t n, float world_w, float world_h,
+                          uint32_t width_px, uint32_t height_px, uint32_t* cover,
+                          uint8_t* image, cudaStream_t st);
 
 }  // namespace wrach
