@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--profile-frames", type=int, default=10)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--workload", default="lattice", choices=["lattice", "surrogate", "batch"],
+                   help="lattice: the headline line; surrogate and batch print their own line")
     return p.parse_args()
 
 
@@ -359,10 +361,135 @@ def run_ours(args):
     return 0
 
 
+def run_surrogate(args):
+    """The learned surrogate at the lattice-1M geometry (1M particles,
+    1920x1080 px, cell 1 px, extended physics, 4 iterations, gravity 0.1).
+    The network is trained on plain-solver frames of the trajectory, then
+    1000 frames are timed twice from the same initial state: plain frames
+    (graph-launched) and surrogate frames (one fused features + network +
+    correction pass and the last plain iteration, the gate on the device:
+    fallback when the mean overlap exceeds the latest plain frame's by 0.2 px
+    or the kinetic energy deviates by 1%; every 32nd frame a plain
+    calibration frame)."""
+    import numpy as np
+    import torch
+    import wrach_gb300 as W
+    W.build()
+    dims, pos, vel, cfg, desc = workload()
+    n = len(pos)
+    sim = W.Simulation(W.WrachConfig(dimensions=dims, **cfg))
+    sim.add_particles(pos, vel)
+    sim.surrogate_init(0, 24 * n)
+    t0 = time.perf_counter()
+    for f in range(480):
+        if f % 20 == 0:
+            sim.surrogate_collect()
+        sim.step(1)
+    sim.sync()
+    collect_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = sim.surrogate_train(4000, 16384, 2e-3)
+    train_s = time.perf_counter() - t0
+    net, zero = sim.surrogate_evaluate()
+    frames = 1000 if args.steps >= 1000 else max(64, args.steps)
+    stream = torch.cuda.ExternalStream(sim.stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
+    def timed(fn):
+        sim.set_particles(pos, vel)
+        sim.sync()
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        out = fn()
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[1]) / 1000.0, out
+
+    sim.set_particles(pos, vel)
+    sim.step(3)                        # the plain frame graphs
+    sim.surrogate_step(3, 0.2, 0.01)   # the fused kernel's set-up
+    plain_s, _ = timed(lambda: sim.step(frames))
+    pen_plain = sim.frame_metrics()
+    sur_s, st = timed(lambda: sim.surrogate_step(frames, 0.2, 0.01))
+    pen_sur = sim.frame_metrics()
+    line = {"metric": "particle-steps/s at 1M particles, surrogate frames (gated) vs plain frames",
+            "value": n * frames / sur_s, "unit": "particle-steps/s", "n_gpus": 1, "steps": frames,
+            "higher_is_better": True, "dtype": "bf16 network / f32 physics", "data": "synthetic",
+            "config": dict(desc, workload="lattice-1M surrogate"),
+            "plain": {"value": n * frames / plain_s, "ms_per_step": 1000 * plain_s / frames},
+            "surrogate": {"ms_per_step": 1000 * sur_s / frames, "frames": st["frames"],
+                          "calibrations": st["calibrations"], "fallbacks": st["fallbacks"],
+                          "mean_penetration_before_last_iteration_px": st["mean_penetration"],
+                          "reference_penetration_px": st["reference_penetration"],
+                          "max_energy_drift": st["max_energy_drift"]},
+            "speedup_vs_plain": plain_s / sur_s,
+            "final_frame": {"plain_mean_penetration_px": pen_plain[0],
+                            "surrogate_mean_penetration_px": pen_sur[0],
+                            "excess_penetration_px": pen_sur[0] - pen_plain[0],
+                            "plain_kinetic_energy": pen_plain[2],
+                            "surrogate_kinetic_energy": pen_sur[2],
+                            "kinetic_energy_ratio": pen_sur[2] / pen_plain[2] if pen_plain[2] else None},
+            "training": {"samples": 24 * n, "frames": 480, "steps": 4000, "batch": 16384,
+                         "final_loss": loss, "collect_s": collect_s, "train_s": train_s,
+                         "held_out_mse_ratio_vs_no_network": net / zero if zero else None}}
+    sim.close()
+    print(json.dumps(line))
+    return 0
+
+
+def run_batch(args):
+    """Config 3: 256 independent worlds (sides U[128, 1024], counts
+    log-uniform in [1024, 65536]) stepped together, launch shape and cell size
+    picked by the autotuner."""
+    import numpy as np
+    import torch
+    import wrach_gb300 as W
+    from wrach_gb300 import autotune, workloads
+    W.build()
+    dims, poss, vels = workloads.batch()
+    n = int(sum(len(p) for p in poss))
+    cfg = W.WrachConfig(cell_size=1, mode=1, iterations=4, gravity=0.1,
+                        capacity=int(max(len(p) for p in poss)))
+    t0 = time.perf_counter()
+    tuned, table = autotune.tune(cfg, poss, vels, worlds=dims.tolist(), frames=6,
+                                 cell_sizes=(1, 2), use_cache=False)
+    tune_s = time.perf_counter() - t0
+    sim = W.Simulation(tuned, worlds=dims.tolist())
+    for w, (p, v) in enumerate(zip(poss, vels)):
+        sim.set_particles(p, v, world=w)
+    stream = torch.cuda.ExternalStream(sim.stream)
+    sim.step(max(3, args.warmup))
+    torch.cuda.synchronize()
+    steps = max(10, min(args.steps, 500))
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    sim.step(steps)
+    end.record(stream)
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    st = sim.stats()
+    line = {"metric": "particle-steps/s, 256 batched worlds", "value": n * steps / (ms / 1000.0),
+            "unit": "particle-steps/s", "n_gpus": 1, "steps": steps, "ms_per_step": ms / steps,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch-256", "worlds": len(poss), "particles": n,
+                       "cells": st["cells"], "physics": "extended (4 iterations, gravity 0.1)",
+                       "l2": "working set above L2 (tables of %d cells)" % st["cells"]},
+            "autotune": {"choice": {"cell_size": tuned.cell_size, "rebin_blocks": tuned.rebin_blocks,
+                                    "solve_block": tuned.solve_block},
+                         "ms_per_frame": table, "seconds": tune_s}}
+    sim.close()
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "surrogate":
+        return run_surrogate(args)
+    if args.workload == "batch":
+        return run_batch(args)
     return run_ours(args)
 
 

@@ -217,15 +217,26 @@ const char *wrach_last_error(WrachContext *ctx);
  * position correction of the first iterations-1 Jacobi iterations of the
  * extended solve.  A surrogate frame applies that correction, runs the last
  * plain iteration (with integration, walls and clamp) and falls back to the
- * plain solve when the frame's mean penetration or kinetic-energy drift
- * exceeds the given bounds.  Extended mode with iterations >= 2 only. */
+ * plain solve of the same frame when its gate fails.  The gate is decided on
+ * the device (no host synchronisation per frame) from metrics the last
+ * iteration computes on its input: the mean over taking-part particles of
+ * the deepest overlap max(0, min_distance - distance) with a neighbour, and
+ * the kinetic energy of the output.  A frame falls back when that mean
+ * exceeds the same measure of the latest plain frame by more than
+ * max_penetration (px), or when its kinetic energy deviates from the plain
+ * frame's by more than max_energy_drift (relative).  Every 32nd frame, the
+ * first included, is a plain calibration frame that refreshes the
+ * reference.  Extended mode with iterations >= 2 only. */
 typedef struct WrachSurrogateStats {
-  uint32_t frames;
-  uint32_t fallbacks;
-  float mean_penetration;  /* mean over frames of the mean deepest overlap */
-  float max_penetration;   /* deepest overlap seen (px) */
+  uint32_t frames;         /* frames run, calibration frames included */
+  uint32_t fallbacks;      /* surrogate frames replaced by the plain solve */
+  float mean_penetration;  /* mean over frames of the mean deepest overlap
+                              before the last iteration (px) */
+  float max_penetration;   /* deepest such overlap in an accepted frame (px) */
   float max_energy_drift;  /* largest relative kinetic-energy deviation */
-  uint32_t reserved[11];
+  uint32_t calibrations;   /* plain calibration frames */
+  float reference_penetration; /* the latest plain frame's mean overlap */
+  uint32_t reserved[9];
 } WrachSurrogateStats;
 
 /* Parameters: w1 [64][64], b1 [64], w2 [64][64], b2 [64], w3 [64][8],
@@ -263,7 +274,19 @@ int wrach_surrogate_train(WrachContext *ctx, uint32_t steps, uint32_t batch,
  * a zero correction (the frame without the network). */
 int wrach_surrogate_evaluate(WrachContext *ctx, float *mse_network,
                              float *mse_zero);
-/* nsteps surrogate frames with the plain fallback gate; blocks per frame. */
+/* Metrics of the current (binned) frame: over the particles that take part
+ * in the solve, the mean and the largest deepest overlap with a neighbour of
+ * the 3x3 cells (min_distance - distance, if positive), and the total
+ * kinetic energy.  Blocks.  No counterpart in the reference. */
+int wrach_frame_metrics(WrachContext *ctx, float *mean_penetration,
+                        float *max_penetration, float *kinetic_energy);
+/* The network's correction of the current binned frame, computed by the
+ * fused kernel of surrogate frames (features, network and correction in one
+ * pass), into d_corr (device, (n, 2) FP32; zero for particles that do not
+ * take part).  Asynchronous on the context's stream. */
+int wrach_surrogate_correction(WrachContext *ctx, float *d_corr);
+/* nsteps frames with the surrogate and its fallback gate; blocks once, at
+ * the end. */
 int wrach_surrogate_step(WrachContext *ctx, uint32_t nsteps,
                          float max_penetration, float max_energy_drift,
                          WrachSurrogateStats *stats);

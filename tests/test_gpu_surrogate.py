@@ -111,16 +111,83 @@ def test_fallback_gate(W):
         sur.add_particles(pos, vel)
         plain.add_particles(pos, vel)
         sur.surrogate_init(3, 16)
-        # a bound nothing can meet: every frame falls back to the plain solve,
-        # which must then equal plain frames bit for bit
-        st = sur.surrogate_step(6, max_penetration=-1.0, max_energy_drift=1e9)
-        plain.step(6)
-        assert st["frames"] == 6 and st["fallbacks"] == 6
+        # a bound nothing can meet: frame 0 is a plain calibration frame and
+        # every other frame falls back to the plain solve, so the run must
+        # equal plain frames bit for bit
+        st = sur.surrogate_step(40, max_penetration=-1.0, max_energy_drift=1e9)
+        plain.step(40)
+        assert st["frames"] == 40 and st["calibrations"] == 2 and st["fallbacks"] == 38
         a, b = sur.read_frame(), plain.read_frame()
         assert np.array_equal(a[2], b[2]) and same_bits(a[0], b[0]) and same_bits(a[1], b[1])
+        # the reference overlap is the plain frames' own measure
+        assert st["reference_penetration"] > 0.0
         # a bound nothing exceeds: no fallback, and a consistent frame
         st = sur.surrogate_step(6, max_penetration=1e9, max_energy_drift=1e9)
-        assert st["frames"] == 6 and st["fallbacks"] == 0
+        assert st["frames"] == 6 and st["calibrations"] == 1 and st["fallbacks"] == 0
         p, v, t = sur.read_frame()
         assert int(t[-1]) == len(pos) and np.all(np.diff(t.astype(np.int64)) >= 0)
         assert st["max_energy_drift"] < 0.01
+
+
+def test_fused_correction_matches_the_separate_kernels(W):
+    # the fused kernel of surrogate frames (features in shared memory, the
+    # network, the correction) against features -> network through global
+    # memory; zero for particles that do not take part
+    torch = _torch()
+    rng = np.random.default_rng(4)
+    dims = (90.0, 50.0)
+    pos = rng.uniform((0, 0), dims, size=(3000, 2)).astype(np.float32)
+    pos[:200] = (30.0 + rng.uniform(-1.5, 1.5, (200, 2))).astype(np.float32)  # over-full cells
+    vel = rng.normal(0, 0.7, size=pos.shape).astype(np.float32)
+    with _sim(W, dims, 8000) as sim:
+        sim.add_particles(pos, vel)
+        sim.surrogate_init(0, 16)
+        sim.surrogate_set_params(_random_net(rng))
+        p, v, table = sim.read_frame()
+        n = len(p)
+        x = torch.zeros((n, 64), dtype=torch.int16, device="cuda")
+        y = torch.zeros((n, 2), dtype=torch.float32, device="cuda")
+        c = torch.full((n, 2), 7.0, dtype=torch.float32, device="cuda")
+        sim.surrogate_features(x.data_ptr(), n)
+        sim.surrogate_forward(x.data_ptr(), n, y.data_ptr())
+        sim.surrogate_correction(c.data_ptr())
+        sim.sync()
+        start = np.asarray(table, np.int64)[1:]
+        cells = np.repeat(np.arange(len(start) - 1), np.diff(start))
+        takes = (np.arange(n) - start[cells]) < 9
+        assert 0 < takes.sum() < n
+        want = np.where(takes[:, None], y.cpu().numpy(), 0.0)
+        got = c.cpu().numpy()
+        np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
+
+
+def test_frame_metrics_match_numpy(W):
+    rng = np.random.default_rng(5)
+    dims = (40.0, 30.0)
+    pos = rng.uniform((0, 0), dims, size=(1400, 2)).astype(np.float32)
+    pos[:100] = (12.0 + rng.uniform(-1.0, 1.0, (100, 2))).astype(np.float32)
+    vel = rng.normal(0, 0.7, size=pos.shape).astype(np.float32)
+    with _sim(W, dims, 4000) as sim:
+        sim.add_particles(pos, vel)
+        mean, mx, ke = sim.frame_metrics()
+        p, v, table = sim.read_frame()
+        s = sim.settings()
+        gx, gy = s.grid_dimensions
+    start = np.asarray(table, np.int64)[1:]
+    pens = []
+    for c in range(gx * gy):
+        cy, cx = divmod(c, gx)
+        cand = []
+        for ny in range(max(cy - 1, 0), min(cy + 1, gy - 1) + 1):
+            for nx in range(max(cx - 1, 0), min(cx + 1, gx - 1) + 1):
+                js, je = start[ny * gx + nx], start[ny * gx + nx + 1]
+                cand.extend(range(js, min(je, js + 9)))
+        cand = np.asarray(cand, np.int64)
+        for i in range(start[c], min(start[c + 1], start[c] + 9)):
+            j = cand[cand != i]
+            d = np.sqrt(((p[j] - p[i]).astype(np.float64) ** 2).sum(1))
+            pens.append(max(0.0, (1.0 - d).max()) if len(j) else 0.0)
+    pens = np.asarray(pens)
+    assert abs(mean - pens.mean()) <= 1e-5 * max(pens.mean(), 1e-3)
+    assert abs(mx - pens.max()) <= 1e-6
+    assert abs(ke - 0.5 * (v.astype(np.float64) ** 2).sum()) <= 1e-5 * ke

@@ -78,7 +78,8 @@ class Stats(ctypes.Structure):
 class SurrogateStats(ctypes.Structure):
     _fields_ = [("frames", ctypes.c_uint32), ("fallbacks", ctypes.c_uint32),
                 ("mean_penetration", ctypes.c_float), ("max_penetration", ctypes.c_float),
-                ("max_energy_drift", ctypes.c_float), ("reserved", ctypes.c_uint32 * 11)]
+                ("max_energy_drift", ctypes.c_float), ("calibrations", ctypes.c_uint32),
+                ("reference_penetration", ctypes.c_float), ("reserved", ctypes.c_uint32 * 9)]
 
 
 # name -> (restype, argtypes); every symbol include/wrach.h declares
@@ -122,6 +123,8 @@ SIGNATURES = {
     "wrach_surrogate_gradients": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _F, _F]),
     "wrach_surrogate_collect": (ctypes.c_int, [_P, _U]),
     "wrach_surrogate_evaluate": (ctypes.c_int, [_P, _F, _F]),
+    "wrach_frame_metrics": (ctypes.c_int, [_P, _F, _F, _F]),
+    "wrach_surrogate_correction": (ctypes.c_int, [_P, _P]),
     "wrach_surrogate_train": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _F]),
     "wrach_surrogate_step": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
                                             ctypes.POINTER(SurrogateStats)]),

@@ -217,6 +217,13 @@ class Simulation:
         t = [int(buf[i]) for i in range(cnt.value)]
         return [b - a for a, b in zip(t, t[1:])]
 
+    def frame_metrics(self):
+        """(mean penetration, max penetration, kinetic energy) of the frame."""
+        a, b, c = ctypes.c_float(0), ctypes.c_float(0), ctypes.c_float(0)
+        self._check(self._L.wrach_frame_metrics(self._ctx, ctypes.byref(a), ctypes.byref(b),
+                                                ctypes.byref(c)))
+        return float(a.value), float(b.value), float(c.value)
+
     # -- the learned surrogate ------------------------------------------------
     def surrogate_init(self, seed=0, max_samples=1 << 20):
         self._check(self._L.wrach_surrogate_init(self._ctx, int(seed), int(max_samples)))
@@ -263,6 +270,11 @@ class Simulation:
         self._check(self._L.wrach_surrogate_train(self._ctx, int(steps), int(batch), float(lr),
                                                   ctypes.byref(loss)))
         return float(loss.value)
+
+    def surrogate_correction(self, d_corr):
+        """The fused kernel's correction of the current frame into the device
+        buffer `d_corr` ((n, 2) float32)."""
+        self._check(self._L.wrach_surrogate_correction(self._ctx, ctypes.c_void_p(int(d_corr))))
 
     def surrogate_step(self, nsteps=1, max_penetration=0.2, max_energy_drift=0.01):
         st = _lib.SurrogateStats()

@@ -24,6 +24,18 @@ NVCC_FLAGS = ARCH + [
 ]
 
 
+# The network kernels are checked against the oracle within a BF16
+# tolerance, not bit for bit, so they may contract multiply-adds; the parts of
+# surrogate.cu that must be exact (features, overlaps) round each operation
+# explicitly (__fmul_rn / __fadd_rn are never contracted).
+FILE_FLAGS = {"surrogate.cu": {"-fmad=false": "-fmad=true"}}
+
+
+def flags_for(src):
+    swap = FILE_FLAGS.get(os.path.basename(src), {})
+    return [swap.get(f, f) for f in NVCC_FLAGS]
+
+
 def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
@@ -52,7 +64,7 @@ def build(force=False, verbose=False):
     for src in sources():
         obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
-        cmd = [nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj]
+        cmd = [nvcc()] + flags_for(src) + ["-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd))
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))

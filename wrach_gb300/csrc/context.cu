@@ -130,6 +130,8 @@ struct WrachContext {
     wrach::MlpDev m{};
     float *params = nullptr, *grad = nullptr, *mom1 = nullptr, *mom2 = nullptr;
     float *loss = nullptr, *metrics = nullptr;
+    float* part = nullptr;           // per-block metrics of a solve launch (8 floats a block)
+    wrach::GateState* gate = nullptr;
     uint16_t* bf16 = nullptr;        // the six BF16 weight arrays
     uint16_t* x = nullptr;           // features of the frame (capacity rows)
     float2* corr = nullptr;          // the network's output (capacity)
@@ -181,7 +183,7 @@ void release(WrachContext* ctx) {
   {
     void* sp[] = {ctx->sur.params, ctx->sur.grad, ctx->sur.mom1, ctx->sur.mom2, ctx->sur.loss,
                   ctx->sur.metrics, ctx->sur.bf16, ctx->sur.x, ctx->sur.corr, ctx->sur.tx,
-                  ctx->sur.tt};
+                  ctx->sur.tt, ctx->sur.part, ctx->sur.gate};
     for (void* p : sp) dfree(p);
   }
   void* ptrs[] = {ctx->worlds_d, ctx->pos, ctx->vel, ctx->pos_o, ctx->vel_o,
@@ -869,6 +871,47 @@ int wrach_surrogate_evaluate(WrachContext* ctx, float* mse_network, float* mse_z
   return WRACH_OK;
 }
 
+// The metric buffers: 8 floats of sums, per-block partials for a solve
+// launch of up to total_cap / 32 blocks, and the gate state.
+int ensure_metrics(WrachContext* ctx) {
+  auto& S = ctx->sur;
+  if (!S.metrics) CK(dalloc(&S.metrics, 8));
+  if (!S.part) CK(dalloc(&S.part, ((size_t)ctx->total_cap / 32 + 2) * 8));
+  if (!S.gate) CK(dalloc(&S.gate, 1));
+  return WRACH_OK;
+}
+
+int wrach_frame_metrics(WrachContext* ctx, float* mean_penetration, float* max_penetration,
+                        float* kinetic_energy) {
+  if (!ctx || !mean_penetration || !max_penetration || !kinetic_energy)
+    return WRACH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(ctx->device);
+  int rc = ensure_metrics(ctx);
+  if (rc) return rc;
+  wrach::SolveArgs a = solve_args(ctx);
+  CK(wrach::launch_penetration(a, ctx->pos, ctx->vel, ctx->sur.part, ctx->sur.metrics, ctx->stream));
+  float h[8];
+  CK(cudaMemcpyAsync(h, ctx->sur.metrics, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->launches += ctx->n ? 2 : 1;
+  *mean_penetration = h[2] > 0.f ? h[0] / h[2] : 0.f;
+  *max_penetration = h[1];
+  *kinetic_energy = h[3];
+  return WRACH_OK;
+}
+
+int wrach_surrogate_correction(WrachContext* ctx, float* d_corr) {
+  int rc = surrogate_ready(ctx);
+  if (rc) return rc;
+  if (!d_corr && ctx->n) return WRACH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(ctx->device);
+  wrach::SolveArgs a = solve_args(ctx);
+  CK(wrach::launch_surrogate_correct(ctx->sur.m, a, ctx->q1, reinterpret_cast<float2*>(d_corr),
+                                     ctx->sur.blocks, ctx->stream));
+  ctx->launches += ctx->n ? 1 : 0;
+  return WRACH_OK;
+}
+
 int wrach_surrogate_train(WrachContext* ctx, uint32_t steps, uint32_t batch, float lr, float* loss) {
   int rc = surrogate_ready(ctx);
   if (rc) return rc;
@@ -895,60 +938,86 @@ int wrach_surrogate_train(WrachContext* ctx, uint32_t steps, uint32_t batch, flo
   return WRACH_OK;
 }
 
+// The rebin of a frame whose solve output is in pos_o / vel_o / keys.
+int enqueue_rebin(WrachContext* ctx) {
+  wrach::RebinArgs r = rebin_args(ctx);
+  r.n = ctx->n;
+  r.dst_capacity = ctx->total_cap;
+  r.pos_src = ctx->pos_o;
+  r.vel_src = ctx->vel_o;
+  r.cs_new = ctx->cs[ctx->cur ^ 1];
+  r.pos_dst = ctx->pos;
+  r.vel_dst = ctx->vel;
+  r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
+  r.force_general = 0;
+  CK(wrach::launch_rebin(r, ctx->rebin_grid, ctx->stream));
+  ctx->launches += 1;
+  ctx->cur ^= 1;
+  return WRACH_OK;
+}
+
+// The plain extended solve of the binned frame into pos_o / vel_o / keys;
+// the final pass writes the gate metrics when `a.part` is set.
+int enqueue_plain_solve(WrachContext* ctx, const wrach::SolveArgs& a) {
+  wrach::SolveArgs inner = a;
+  inner.part = nullptr;
+  const float2* src = ctx->pos;
+  for (uint32_t it = 0; it + 1 < ctx->ph.iterations; ++it) {
+    float2* dst = (it & 1) ? ctx->q2 : ctx->q1;
+    CK(wrach::launch_solve_extended(inner, src, dst, false, 1, ctx->stream));
+    src = dst;
+  }
+  CK(wrach::launch_solve_extended(a, src, ctx->pos_o, true, 1, ctx->stream));
+  ctx->launches += ctx->ph.iterations;
+  return WRACH_OK;
+}
+
+constexpr uint32_t kCalibrationPeriod = 32;
+
 int wrach_surrogate_step(WrachContext* ctx, uint32_t nsteps, float max_penetration,
                          float max_energy_drift, WrachSurrogateStats* stats) {
   int rc = surrogate_ready(ctx);
   if (rc) return rc;
   DeviceGuard guard(ctx->device);
+  if ((rc = ensure_metrics(ctx))) return rc;
   auto& S = ctx->sur;
-  WrachSurrogateStats st{};
-  double pen_sum = 0.0;
+  wrach::GateState g0{};
+  g0.tol = max_penetration;
+  g0.max_drift = max_energy_drift;
+  CK(cudaMemcpyAsync(S.gate, &g0, sizeof(g0), cudaMemcpyHostToDevice, ctx->stream));
   for (uint32_t f = 0; f < nsteps; ++f) {
     wrach::SolveArgs a = solve_args(ctx);
-    // surrogate correction, then the last iteration of the plain solve
-    CK(wrach::launch_knn_features(a, S.x, ctx->stream));
-    CK(wrach::launch_mlp_forward(S.m, S.x, ctx->n, S.corr, S.blocks, ctx->stream));
-    CK(wrach::launch_apply_correction(a, S.corr, ctx->q1, ctx->stream));
-    CK(wrach::launch_solve_extended(a, ctx->q1, ctx->pos_o, true, 1, ctx->stream));
-    CK(cudaMemsetAsync(S.metrics, 0, 8 * 4, ctx->stream));
-    CK(wrach::launch_penetration(a, ctx->pos_o, ctx->vel_o, S.metrics, ctx->stream));
-    float h[8];
-    CK(cudaMemcpyAsync(h, S.metrics, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-    ctx->launches += 5;
-    const float mean_pen = h[2] > 0.f ? h[0] / h[2] : 0.f;
-    const float drift = h[4] > 0.f ? std::fabs(h[3] - h[4]) / h[4] : 0.f;
-    st.max_penetration = std::max(st.max_penetration, h[1]);
-    st.max_energy_drift = std::max(st.max_energy_drift, drift);
-    pen_sum += mean_pen;
-    if (mean_pen > max_penetration || drift > max_energy_drift) {
-      // fallback: the plain solve of the same frame overwrites the output
-      ++st.fallbacks;
-      const float2* src = ctx->pos;
-      for (uint32_t it = 0; it + 1 < ctx->ph.iterations; ++it) {
-        float2* dst = (it & 1) ? ctx->q2 : ctx->q1;
-        CK(wrach::launch_solve_extended(a, src, dst, false, 1, ctx->stream));
-        src = dst;
-      }
-      CK(wrach::launch_solve_extended(a, src, ctx->pos_o, true, 1, ctx->stream));
-      ctx->launches += ctx->ph.iterations;
+    a.part = S.part;
+    const uint32_t nparts = wrach::solve_blocks(a);
+    if (f % kCalibrationPeriod == 0) {
+      // a plain frame: its metrics are the reference of the next frames
+      if ((rc = enqueue_plain_solve(ctx, a))) return rc;
+      CK(wrach::launch_gate(S.part, nparts, S.gate, 2, ctx->stream));
+    } else {
+      // the surrogate correction, the last plain iteration, the gate
+      CK(wrach::launch_surrogate_correct(S.m, a, ctx->q1, nullptr, S.blocks, ctx->stream));
+      CK(wrach::launch_solve_extended(a, ctx->q1, ctx->pos_o, true, 1, ctx->stream));
+      CK(wrach::launch_gate(S.part, nparts, S.gate, 0, ctx->stream));
+      // the plain solve of the same frame, run only when the gate failed it
+      a.run_if = &S.gate->fallback;
+      if ((rc = enqueue_plain_solve(ctx, a))) return rc;
+      CK(wrach::launch_gate(S.part, nparts, S.gate, 1, ctx->stream));
+      ctx->launches += 4;
     }
-    wrach::RebinArgs r = rebin_args(ctx);
-    r.n = ctx->n;
-    r.dst_capacity = ctx->total_cap;
-    r.pos_src = ctx->pos_o;
-    r.vel_src = ctx->vel_o;
-    r.cs_new = ctx->cs[ctx->cur ^ 1];
-    r.pos_dst = ctx->pos;
-    r.vel_dst = ctx->vel;
-    r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
-    r.force_general = 0;
-    CK(wrach::launch_rebin(r, ctx->rebin_grid, ctx->stream));
     ctx->launches += 1;
-    ctx->cur ^= 1;
-    ++st.frames;
+    if ((rc = enqueue_rebin(ctx))) return rc;
   }
-  st.mean_penetration = st.frames ? (float)(pen_sum / st.frames) : 0.f;
+  wrach::GateState g{};
+  CK(cudaMemcpyAsync(&g, S.gate, sizeof(g), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  WrachSurrogateStats st{};
+  st.frames = g.frames;
+  st.fallbacks = g.fallbacks;
+  st.calibrations = g.calibrations;
+  st.mean_penetration = g.frames ? g.pen_sum / (float)g.frames : 0.f;
+  st.max_penetration = g.pen_max;
+  st.max_energy_drift = g.drift_max;
+  st.reference_penetration = g.pen_ref;
   if (stats) *stats = st;
   return WRACH_OK;
 }

@@ -92,16 +92,27 @@ k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
 // an over-full cell keep their position.  The neighbour order is fixed (3x3
 // cells in row-major order, table order inside a cell), so the sum is
 // deterministic.  FINAL fuses gravity, integration, boundaries, the velocity
-// clamp and the key emission.
-template <bool FINAL>
+// clamp and the key emission.  METRICS (final pass only) also writes the
+// block's sums for the surrogate's fallback gate to part[blockIdx.x * 8 +
+// k]: [0] sum and [1] max over taking-part particles of the deepest overlap
+// max(0, min_d - distance) with a pushing neighbour (measured on the pass's
+// input), [2] the number of taking-part particles, [3] the kinetic energy of
+// the output and [4] the kinetic energy a plain frame gives (gravity, the
+// clamp and wall reflections only change the velocity).  A launch whose
+// `run_if` flag reads 0 returns at once.
+template <bool FINAL, bool METRICS>
 __global__ void __launch_bounds__(512)
 k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
          uint32_t n, int do_push, const uint32_t* __restrict__ cell_start,
          const uint32_t* __restrict__ cell_of, const float2* __restrict__ qin,
          float2* __restrict__ qout, const float2* __restrict__ vin,
-         float2* __restrict__ vout, uint32_t* __restrict__ keys, Ctrl* ctrl) {
+         float2* __restrict__ vout, uint32_t* __restrict__ keys, Ctrl* ctrl,
+         const uint32_t* __restrict__ run_if, float* __restrict__ part) {
+  static_assert(FINAL || !METRICS, "metrics come from the final pass");
+  if (run_if && *run_if == 0u) return;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t flags = 0;
+  float pen = 0.f, taking = 0.f, ke = 0.f, ke_plain = 0.f;
   if (i < n) {
     const uint32_t c = cell_of[i];
     const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
@@ -110,6 +121,7 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
     const float2 qi = qin[i];
     float ax = 0.0f, ay = 0.0f;
     if (do_push && i - cell_start[c] < ph.cap) {
+      if (METRICS) taking = 1.f;
       // the table entries of the three neighbour rows first: independent
       // loads, so their latencies overlap
       const uint32_t x0 = cx > 0 ? cx - 1 : 0;
@@ -165,8 +177,9 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
           const uint32_t j = (b < 16 ? s0 : (b < 32 ? s1 - 16 : s2 - 32)) + b;
           const float2 qj = qin[j];
           const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
-          float f;
-          if (!push_factor(dx, dy, ph.min_d, ph.skip_d2, f)) continue;
+          float f, d;
+          if (!push_factor(dx, dy, ph.min_d, ph.skip_d2, f, d)) continue;
+          if (METRICS) pen = fmaxf(pen, __fsub_rn(ph.min_d, d));
           ax = __fadd_rn(ax, __fmul_rn(dx, f));
           ay = __fadd_rn(ay, __fmul_rn(dy, f));
         }
@@ -183,9 +196,40 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
       qout[i] = make_float2(px, py);
       vout[i] = make_float2(ux, uy);
       keys[i] = next_key(w, px, py, flags);
+      if (METRICS) {
+        ke = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)));
+        const float cx = fminf(fmaxf(v.x, -ph.vmax), ph.vmax);
+        const float cy = fminf(fmaxf(__fsub_rn(v.y, ph.gravity), -ph.vmax), ph.vmax);
+        ke_plain = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
+      }
     }
   }
   if (FINAL) publish_flags(ctrl, flags);
+  if (METRICS) {
+    // warp sums, then one thread sums the block's warps in a fixed order
+    __shared__ float red[16][5];
+    float v[5] = {pen, pen, taking, ke, ke_plain};
+#pragma unroll
+    for (uint32_t o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const float u = __shfl_xor_sync(0xffffffffu, v[k], o);
+        v[k] = k == 1 ? fmaxf(v[k], u) : __fadd_rn(v[k], u);
+      }
+    }
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < 5; ++k) red[warp][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 5) {
+      const uint32_t nw = (blockDim.x + 31) >> 5;
+      float acc = red[0][threadIdx.x];
+      for (uint32_t w = 1; w < nw; ++w)
+        acc = threadIdx.x == 1 ? fmaxf(acc, red[w][threadIdx.x]) : __fadd_rn(acc, red[w][threadIdx.x]);
+      part[blockIdx.x * 8 + threadIdx.x] = acc;
+    }
+  }
 }
 
 }  // namespace
@@ -206,14 +250,18 @@ cudaError_t launch_solve_extended(const SolveArgs& a, const float2* qin,
   if (a.n == 0) return cudaSuccess;
   const uint32_t threads = a.block ? a.block : 256;
   const uint32_t blocks = (a.n + threads - 1) / threads;
-  if (final_pass)
-    k_jacobi<true><<<blocks, threads, 0, st>>>(
+  if (final_pass && a.part)
+    k_jacobi<true, true><<<blocks, threads, 0, st>>>(
         a.worlds, a.nworlds, a.ph, a.n, do_push, a.cell_start, a.cell_of, qin,
-        qout, a.vel, a.vel_out, a.keys, a.ctrl);
+        qout, a.vel, a.vel_out, a.keys, a.ctrl, a.run_if, a.part);
+  else if (final_pass)
+    k_jacobi<true, false><<<blocks, threads, 0, st>>>(
+        a.worlds, a.nworlds, a.ph, a.n, do_push, a.cell_start, a.cell_of, qin,
+        qout, a.vel, a.vel_out, a.keys, a.ctrl, a.run_if, nullptr);
   else
-    k_jacobi<false><<<blocks, threads, 0, st>>>(
+    k_jacobi<false, false><<<blocks, threads, 0, st>>>(
         a.worlds, a.nworlds, a.ph, a.n, do_push, a.cell_start, a.cell_of, qin,
-        qout, nullptr, nullptr, nullptr, a.ctrl);
+        qout, nullptr, nullptr, nullptr, a.ctrl, a.run_if, nullptr);
   return cudaGetLastError();
 }
 

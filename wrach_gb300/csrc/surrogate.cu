@@ -50,29 +50,38 @@ __device__ __forceinline__ float gelu_grad(float x) {
   return cdf + x * pdf;
 }
 
-// Shared-memory copy of the network: weights as BF16 in two layouts (WT
-// [out][in] for the forward pass, W [in][out] for the backward pass) and the
-// biases in FP32.
+// Shared-memory copy of the network for the forward pass: the weights as
+// BF16 in the [out][in] layout (the B operand, k = in contiguous) and the
+// biases in FP32.  Each row of 64 BF16 (32 words) is padded to kRow = 36
+// words, so that the B-fragment loads of a warp (rows g = 0..7, words t =
+// 0..3) fall in 32 distinct banks: (36 g + t) mod 32 = 4 g + t.
+constexpr uint32_t kRow = kIn / 2 + 4;
+static_assert(kIn == kHid, "one padded row length serves every layer");
 struct SmemNet {
-  uint32_t w1t[kHid * kIn / 2], w2t[kHid * kHid / 2], w3t[kOutPad * kHid / 2];
-  uint32_t w1[kIn * kHid / 2], w2[kHid * kHid / 2], w3[kHid * kOutPad / 2];
+  uint32_t w1t[kHid * kRow], w2t[kHid * kRow], w3t[kOutPad * kRow];
   float b1[kHid], b2[kHid], b3[kOutPad];
 };
+// The [in][out] copies the backward pass multiplies the gradients by.
+struct SmemNetT {
+  uint32_t w1[kIn * kRow], w2[kHid * kRow], w3[kHid * kOutPad / 2];
+};
 
-__device__ void load_net(const MlpDev& m, SmemNet& s, bool backward) {
-  const uint32_t* src;
-  for (uint32_t i = threadIdx.x; i < kHid * kIn / 2; i += blockDim.x) {
-    s.w1t[i] = reinterpret_cast<const uint32_t*>(m.w1t)[i];
-    s.w2t[i] = reinterpret_cast<const uint32_t*>(m.w2t)[i];
-    if (backward) {
-      s.w1[i] = reinterpret_cast<const uint32_t*>(m.w1)[i];
-      s.w2[i] = reinterpret_cast<const uint32_t*>(m.w2)[i];
-    }
-  }
-  src = reinterpret_cast<const uint32_t*>(m.w3t);
-  for (uint32_t i = threadIdx.x; i < kOutPad * kHid / 2; i += blockDim.x) {
-    s.w3t[i] = src[i];
-    if (backward) s.w3[i] = reinterpret_cast<const uint32_t*>(m.w3)[i];
+// rows x 32 words from a packed global array into padded shared rows
+__device__ __forceinline__ void load_rows(uint32_t* dst, const uint16_t* src, uint32_t rows) {
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+  for (uint32_t i = threadIdx.x; i < rows * (kIn / 2); i += blockDim.x)
+    dst[(i / (kIn / 2)) * kRow + i % (kIn / 2)] = s[i];
+}
+
+__device__ void load_net(const MlpDev& m, SmemNet& s, SmemNetT* st) {
+  load_rows(s.w1t, m.w1t, kHid);
+  load_rows(s.w2t, m.w2t, kHid);
+  load_rows(s.w3t, m.w3t, kOutPad);
+  if (st) {
+    load_rows(st->w1, m.w1, kIn);
+    load_rows(st->w2, m.w2, kHid);
+    for (uint32_t i = threadIdx.x; i < kHid * kOutPad / 2; i += blockDim.x)
+      st->w3[i] = reinterpret_cast<const uint32_t*>(m.w3)[i];
   }
   for (uint32_t i = threadIdx.x; i < kHid; i += blockDim.x) {
     s.b1[i] = m.b1[i];
@@ -82,13 +91,12 @@ __device__ void load_net(const MlpDev& m, SmemNet& s, bool backward) {
   __syncthreads();
 }
 
-// B fragment of W^T stored [n][k] (k contiguous, `kdim` columns): k-tile kk,
+// B fragment of a weight matrix stored [n][k] in padded rows: k-tile kk,
 // n-tile nt.
-__device__ __forceinline__ void bfrag(const uint32_t* wt, uint32_t kdim, uint32_t kk,
-                                      uint32_t nt, uint32_t lane, uint32_t& b0,
-                                      uint32_t& b1) {
+__device__ __forceinline__ void bfrag(const uint32_t* wt, uint32_t kk, uint32_t nt,
+                                      uint32_t lane, uint32_t& b0, uint32_t& b1) {
   const uint32_t g = lane >> 2, t = lane & 3;
-  const uint32_t row = (nt * 8 + g) * (kdim / 2);
+  const uint32_t row = (nt * 8 + g) * kRow;
   b0 = wt[row + kk * 8 + t];
   b1 = wt[row + kk * 8 + 4 + t];
 }
@@ -110,7 +118,7 @@ __device__ __forceinline__ void mlp_tile_forward(const SmemNet& s, uint32_t lane
 #pragma unroll
     for (uint32_t kk = 0; kk < 4; ++kk) {
       uint32_t b0, b1;
-      bfrag(s.w1t, kIn, kk, nt, lane, b0, b1);
+      bfrag(s.w1t, kk, nt, lane, b0, b1);
       mma_bf16(z1[nt], ax[kk], b0, b1);
     }
   }
@@ -128,7 +136,7 @@ __device__ __forceinline__ void mlp_tile_forward(const SmemNet& s, uint32_t lane
 #pragma unroll
     for (uint32_t kk = 0; kk < 4; ++kk) {
       uint32_t b0, b1;
-      bfrag(s.w2t, kHid, kk, nt, lane, b0, b1);
+      bfrag(s.w2t, kk, nt, lane, b0, b1);
       mma_bf16(z2[nt], h1[kk], b0, b1);
     }
   }
@@ -145,10 +153,72 @@ __device__ __forceinline__ void mlp_tile_forward(const SmemNet& s, uint32_t lane
 #pragma unroll
     for (uint32_t kk = 0; kk < 4; ++kk) {
       uint32_t b0, b1;
-      bfrag(s.w3t, kHid, kk, 0, lane, b0, b1);
+      bfrag(s.w3t, kk, 0, lane, b0, b1);
       mma_bf16(y, h2[kk], b0, b1);
     }
   }
+}
+
+// A shared-memory word read that the compiler keeps in place (it would
+// otherwise hoist the loop-invariant weight fragments of a persistent loop
+// into registers and lose occupancy).
+__device__ __forceinline__ uint32_t lds_keep(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.shared.b32 %0, [%1];"
+               : "=r"(v)
+               : "r"((uint32_t)__cvta_generic_to_shared(p)));
+  return v;
+}
+
+// The forward pass of a 16-row tile for inference only: the same products
+// in the same order as mlp_tile_forward (bit-identical outputs), computed two
+// n-tiles at a time so that no pre-activation array stays live.
+__device__ __forceinline__ void mlp_tile_infer(const SmemNet& s, uint32_t lane,
+                                               const uint32_t (&ax)[4][4], float (&y)[4]) {
+  const uint32_t g = lane >> 2, t = lane & 3;
+  uint32_t h1[4][4], h2[4][4];
+#pragma unroll
+  for (uint32_t kq = 0; kq < 4; ++kq) {
+    float z[2][4];
+#pragma unroll
+    for (uint32_t u = 0; u < 2; ++u) {
+      const uint32_t nt = 2 * kq + u;
+      const float bl = s.b1[nt * 8 + 2 * t], bh = s.b1[nt * 8 + 2 * t + 1];
+      z[u][0] = bl; z[u][1] = bh; z[u][2] = bl; z[u][3] = bh;
+      const uint32_t* row = s.w1t + (nt * 8 + g) * kRow + t;
+#pragma unroll
+      for (uint32_t kk = 0; kk < 4; ++kk)
+        mma_bf16(z[u], ax[kk], lds_keep(row + kk * 8), lds_keep(row + kk * 8 + 4));
+    }
+    h1[kq][0] = pack_bf16(gelu(z[0][0]), gelu(z[0][1]));
+    h1[kq][1] = pack_bf16(gelu(z[0][2]), gelu(z[0][3]));
+    h1[kq][2] = pack_bf16(gelu(z[1][0]), gelu(z[1][1]));
+    h1[kq][3] = pack_bf16(gelu(z[1][2]), gelu(z[1][3]));
+  }
+#pragma unroll
+  for (uint32_t kq = 0; kq < 4; ++kq) {
+    float z[2][4];
+#pragma unroll
+    for (uint32_t u = 0; u < 2; ++u) {
+      const uint32_t nt = 2 * kq + u;
+      const float bl = s.b2[nt * 8 + 2 * t], bh = s.b2[nt * 8 + 2 * t + 1];
+      z[u][0] = bl; z[u][1] = bh; z[u][2] = bl; z[u][3] = bh;
+      const uint32_t* row = s.w2t + (nt * 8 + g) * kRow + t;
+#pragma unroll
+      for (uint32_t kk = 0; kk < 4; ++kk)
+        mma_bf16(z[u], h1[kk], lds_keep(row + kk * 8), lds_keep(row + kk * 8 + 4));
+    }
+    h2[kq][0] = pack_bf16(gelu(z[0][0]), gelu(z[0][1]));
+    h2[kq][1] = pack_bf16(gelu(z[0][2]), gelu(z[0][3]));
+    h2[kq][2] = pack_bf16(gelu(z[1][0]), gelu(z[1][1]));
+    h2[kq][3] = pack_bf16(gelu(z[1][2]), gelu(z[1][3]));
+  }
+  const float bl = s.b3[2 * t], bh = s.b3[2 * t + 1];
+  y[0] = bl; y[1] = bh; y[2] = bl; y[3] = bh;
+  const uint32_t* row = s.w3t + g * kRow + t;
+#pragma unroll
+  for (uint32_t kk = 0; kk < 4; ++kk)
+    mma_bf16(y, h2[kk], lds_keep(row + kk * 8), lds_keep(row + kk * 8 + 4));
 }
 
 // A fragment (4 k-tiles) of 16 rows of X (BF16 [rows][64]); rows past n read
@@ -171,15 +241,15 @@ __device__ __forceinline__ void load_x_tile(const uint16_t* x, uint32_t row0, ui
 __global__ void __launch_bounds__(128) k_mlp_forward(MlpDev m, const uint16_t* __restrict__ x,
                                                      uint32_t n, float2* __restrict__ y) {
   __shared__ SmemNet s;
-  load_net(m, s, false);
+  load_net(m, s, nullptr);
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t g = lane >> 2, t = lane & 3;
   const uint32_t tiles = (n + 15) / 16;
   for (uint32_t tile = blockIdx.x * 4 + warp; tile < tiles; tile += gridDim.x * 4) {
-    uint32_t ax[4][4], h1[4][4], h2[4][4];
-    float z1[8][4], z2[8][4], out[4];
+    uint32_t ax[4][4];
+    float out[4];
     load_x_tile(x, tile * 16, n, lane, ax);
-    mlp_tile_forward(s, lane, ax, z1, h1, z2, h2, out);
+    mlp_tile_infer(s, lane, ax, out);
     if (t == 0) {
       const uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
       if (r0 < n) y[r0] = make_float2(out[0], out[1]);
@@ -277,9 +347,11 @@ __global__ void __launch_bounds__(128) k_mlp_backward(MlpDev m, const uint16_t* 
                                                       float* __restrict__ loss) {
   extern __shared__ __align__(16) uint8_t dyn[];
   SmemNet& s = *reinterpret_cast<SmemNet*>(dyn);
-  SmemGrad& acc = *reinterpret_cast<SmemGrad*>(dyn + sizeof(SmemNet));
-  SmemBack* back = reinterpret_cast<SmemBack*>(dyn + sizeof(SmemNet) + sizeof(SmemGrad));
-  load_net(m, s, true);
+  SmemNetT& st = *reinterpret_cast<SmemNetT*>(dyn + sizeof(SmemNet));
+  SmemGrad& acc = *reinterpret_cast<SmemGrad*>(dyn + sizeof(SmemNet) + sizeof(SmemNetT));
+  SmemBack* back =
+      reinterpret_cast<SmemBack*>(dyn + sizeof(SmemNet) + sizeof(SmemNetT) + sizeof(SmemGrad));
+  load_net(m, s, &st);
   float* accf = reinterpret_cast<float*>(&acc);
   for (uint32_t i = threadIdx.x; i < sizeof(SmemGrad) / 4; i += blockDim.x) accf[i] = 0.f;
   __syncthreads();
@@ -323,7 +395,7 @@ __global__ void __launch_bounds__(128) k_mlp_backward(MlpDev m, const uint16_t* 
     for (uint32_t nt = 0; nt < 8; ++nt) {
       dz2[nt][0] = dz2[nt][1] = dz2[nt][2] = dz2[nt][3] = 0.f;
       // B(k = out, n = in) = W3[in][out]; W3 stored [in][8]
-      const uint32_t b0 = s.w3[(nt * 8 + g) * (kOutPad / 2) + t];
+      const uint32_t b0 = st.w3[(nt * 8 + g) * (kOutPad / 2) + t];
       mma_bf16(dz2[nt], ady, b0, 0u);
     }
 #pragma unroll
@@ -346,7 +418,7 @@ __global__ void __launch_bounds__(128) k_mlp_backward(MlpDev m, const uint16_t* 
 #pragma unroll
       for (uint32_t kk = 0; kk < 4; ++kk) {
         uint32_t b0, b1;
-        bfrag(s.w2, kHid, kk, nt, lane, b0, b1);  // W2 [in][out]: B(k=out, n=in)
+        bfrag(st.w2, kk, nt, lane, b0, b1);  // W2 [in][out]: B(k=out, n=in)
         mma_bf16(dz1[nt], adz2[kk], b0, b1);
       }
     }
@@ -422,7 +494,7 @@ __global__ void __launch_bounds__(128) k_mlp_backward(MlpDev m, const uint16_t* 
 }
 
 size_t backward_smem() {
-  return sizeof(SmemNet) + sizeof(SmemGrad) + 4 * sizeof(SmemBack);
+  return sizeof(SmemNet) + sizeof(SmemNetT) + sizeof(SmemGrad) + 4 * sizeof(SmemBack);
 }
 
 // Adam on the FP32 master parameters (the SmemGrad order), then the BF16
@@ -478,23 +550,24 @@ __global__ void k_adam(MlpDev m, const float* __restrict__ grad, float* __restri
 
 constexpr uint32_t kK = kKnn;
 
-// Features of the binned state (one thread per particle): the 12 nearest
-// taking-part particles (the first `cap` of each cell) in the 5x5 cells
-// around the particle's cell, by squared distance, ties by index; each as
-// (dx, dy, dvx, dvy); then the own velocity; zero padding to 64.  Particles
-// that do not take part (past the capacity of their cell) get all zeros.
-__global__ void __launch_bounds__(256)
-k_knn_features(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32_t n,
-               const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ cell_of,
-               const float2* __restrict__ pos, const float2* __restrict__ vel,
-               uint16_t* __restrict__ x) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  uint32_t* row = reinterpret_cast<uint32_t*>(x + (size_t)i * kIn);
+// Features of particle i into `row` (32 words, global or shared memory): the
+// 12 nearest taking-part particles (the first `cap` of each cell) in the 5x5
+// cells around the particle's cell, by binary32 squared distance (each
+// product and sum rounded on its own), ties by index; each as (dx, dy, dvx,
+// dvy) relative to the particle; then the own velocity; zero padding to 64.
+// A particle that does not take part (past the capacity of its cell) gets
+// all zeros.  Returns whether the particle takes part.
+__device__ __forceinline__ bool knn_row(const WorldDev* __restrict__ worlds, int nworlds,
+                                        const PhysDev& ph, const uint32_t* __restrict__ cell_start,
+                                        const uint32_t* __restrict__ cell_of,
+                                        const float2* __restrict__ pos,
+                                        const float2* __restrict__ vel, uint32_t i,
+                                        uint32_t* row) {
   const uint32_t c = cell_of[i];
   if (i - cell_start[c] >= ph.cap) {
+#pragma unroll
     for (uint32_t k = 0; k < kIn / 2; ++k) row[k] = 0u;
-    return;
+    return false;
   }
   const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
   uint32_t cx, cy;
@@ -508,32 +581,36 @@ k_knn_features(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uin
     bj[k] = 0xFFFFFFFFu;
   }
   const int y0 = max((int)cy - 2, 0), y1 = min((int)cy + 2, (int)w.gy - 1);
-  const int x0 = max((int)cx - 2, 0), x1 = min((int)cx + 2, (int)w.gx - 1);
+  const uint32_t x0 = cx >= 2 ? cx - 2 : 0, x1 = min(cx + 2, w.gx - 1);
+  const uint32_t ncol = x1 - x0 + 1;  // 3 to 5 cells per row
   for (int ny = y0; ny <= y1; ++ny) {
-    const uint32_t rb = w.cell_off + (uint32_t)ny * w.gx;
-    for (int nx = x0; nx <= x1; ++nx) {
-      const uint32_t js = cell_start[rb + nx];
-      const uint32_t je = min(cell_start[rb + nx + 1], js + ph.cap);
+    // the row's table entries first: independent loads
+    const uint32_t rb = w.cell_off + (uint32_t)ny * w.gx + x0;
+    uint32_t st[6];
+#pragma unroll
+    for (uint32_t k = 0; k < 6; ++k) st[k] = k <= ncol ? cell_start[rb + k] : 0u;
+#pragma unroll
+    for (uint32_t col = 0; col < 5; ++col) {
+      if (col >= ncol) break;
+      const uint32_t js = st[col], je = min(st[col + 1], js + ph.cap);
       for (uint32_t j = js; j < je; ++j) {
         if (j == i) continue;
         const float2 pj = pos[j];
-        const float dx = pj.x - pi.x, dy = pj.y - pi.y;
-        float d = dx * dx + dy * dy;
+        const float dx = __fsub_rn(pj.x, pi.x), dy = __fsub_rn(pj.y, pi.y);
+        float d = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
         if (!(d < bd[kK - 1]) && !(d == bd[kK - 1] && j < bj[kK - 1])) continue;
-        uint32_t jj = j;
-        // insert, keeping (distance, index) ascending
+        // insert, keeping (distance, index) ascending: every comparison
+        // against the old list first, then the shift (no serial chain)
+        bool lt[kK];
 #pragma unroll
-        for (uint32_t k = 0; k < kK; ++k) {
-          const bool less = d < bd[k] || (d == bd[k] && jj < bj[k]);
-          if (less) {
-            const float td = bd[k];
-            const uint32_t tj = bj[k];
-            bd[k] = d;
-            bj[k] = jj;
-            d = td;
-            jj = tj;
-          }
+        for (uint32_t k = 0; k < kK; ++k) lt[k] = d < bd[k] || (d == bd[k] && j < bj[k]);
+#pragma unroll
+        for (uint32_t k = kK - 1; k > 0; --k) {
+          bd[k] = lt[k - 1] ? bd[k - 1] : (lt[k] ? d : bd[k]);
+          bj[k] = lt[k - 1] ? bj[k - 1] : (lt[k] ? j : bj[k]);
         }
+        bd[0] = lt[0] ? d : bd[0];
+        bj[0] = lt[0] ? j : bj[0];
       }
     }
   }
@@ -541,32 +618,101 @@ k_knn_features(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uin
   for (uint32_t k = 0; k < kK; ++k) {
     if (bj[k] != 0xFFFFFFFFu) {
       const float2 pj = pos[bj[k]], vj = vel[bj[k]];
-      row[2 * k] = pack_bf16(pj.x - pi.x, pj.y - pi.y);
-      row[2 * k + 1] = pack_bf16(vj.x - vi.x, vj.y - vi.y);
+      row[2 * k] = pack_bf16(__fsub_rn(pj.x, pi.x), __fsub_rn(pj.y, pi.y));
+      row[2 * k + 1] = pack_bf16(__fsub_rn(vj.x, vi.x), __fsub_rn(vj.y, vi.y));
     } else {
       row[2 * k] = 0u;
       row[2 * k + 1] = 0u;
     }
   }
   row[2 * kK] = pack_bf16(vi.x, vi.y);
+#pragma unroll
   for (uint32_t k = 2 * kK + 1; k < kIn / 2; ++k) row[k] = 0u;
+  return true;
 }
 
-// q = p + the network's correction for taking-part particles; p otherwise.
-__global__ void k_apply_correction(const WorldDev* __restrict__ worlds, PhysDev ph, uint32_t n,
-                                   const uint32_t* __restrict__ cell_start,
-                                   const uint32_t* __restrict__ cell_of,
-                                   const float2* __restrict__ pos, const float2* __restrict__ corr,
-                                   float2* __restrict__ q) {
+// Features of the binned state into x (BF16 [n][64]), one thread per
+// particle.
+__global__ void __launch_bounds__(256)
+k_knn_features(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32_t n,
+               const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ cell_of,
+               const float2* __restrict__ pos, const float2* __restrict__ vel,
+               uint16_t* __restrict__ x) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float2 p = pos[i];
-  if (i - cell_start[cell_of[i]] >= ph.cap) {
-    q[i] = p;
-    return;
+  knn_row(worlds, nworlds, ph, cell_start, cell_of, pos, vel, i,
+          reinterpret_cast<uint32_t*>(x + (size_t)i * kIn));
+}
+
+// The surrogate correction of a frame in one pass: per tile of 256
+// particles, the features go to shared memory (padded rows, so the A-fragment
+// loads are conflict-free like the weights'), each warp runs the network on
+// 32 of the rows, and the correction is applied on the spot:
+// q = p + correction for taking-part particles, q = p otherwise.  `corr`
+// (optional) receives the correction (zero for particles that do not take
+// part).  Persistent: the network is loaded once per block.
+constexpr uint32_t kFuseThreads = 256;
+
+__global__ void __launch_bounds__(kFuseThreads, 3)
+k_surrogate_correct(MlpDev m, const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
+                    uint32_t n, const uint32_t* __restrict__ cell_start,
+                    const uint32_t* __restrict__ cell_of, const float2* __restrict__ pos,
+                    const float2* __restrict__ vel, float2* __restrict__ q,
+                    float2* __restrict__ corr) {
+  extern __shared__ __align__(16) uint8_t dyn[];
+  SmemNet& s = *reinterpret_cast<SmemNet*>(dyn);
+  uint32_t* sx = reinterpret_cast<uint32_t*>(dyn + sizeof(SmemNet));  // [256][kRow]
+  uint32_t* take = sx + kFuseThreads * kRow;                          // [256]
+  load_net(m, s, nullptr);
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t g = lane >> 2, t = lane & 3;
+  for (uint32_t base = blockIdx.x * kFuseThreads; base < n; base += gridDim.x * kFuseThreads) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t* row = sx + threadIdx.x * kRow;
+    bool tk = false;
+    if (i < n) {
+      tk = knn_row(worlds, nworlds, ph, cell_start, cell_of, pos, vel, i, row);
+    } else {
+#pragma unroll
+      for (uint32_t k = 0; k < kIn / 2; ++k) row[k] = 0u;
+    }
+    take[threadIdx.x] = tk;
+    __syncthreads();
+#pragma unroll 1
+    for (uint32_t rt = 0; rt < 2; ++rt) {
+      const uint32_t r0 = warp * 32 + rt * 16;
+      uint32_t ax[4][4];
+      float out[4];
+      const uint32_t* p0 = sx + (r0 + g) * kRow;
+      const uint32_t* p1 = sx + (r0 + g + 8) * kRow;
+#pragma unroll
+      for (uint32_t kk = 0; kk < 4; ++kk) {
+        ax[kk][0] = p0[kk * 8 + t];
+        ax[kk][1] = p1[kk * 8 + t];
+        ax[kk][2] = p0[kk * 8 + 4 + t];
+        ax[kk][3] = p1[kk * 8 + 4 + t];
+      }
+      mlp_tile_infer(s, lane, ax, out);
+      if (t == 0) {
+#pragma unroll
+        for (uint32_t h = 0; h < 2; ++h) {
+          const uint32_t r = r0 + g + 8 * h, idx = base + r;
+          if (idx < n) {
+            const float2 p = pos[idx];
+            const bool on = take[r] != 0u;
+            const float cxv = on ? out[2 * h] : 0.f, cyv = on ? out[2 * h + 1] : 0.f;
+            if (corr) corr[idx] = make_float2(cxv, cyv);
+            q[idx] = on ? make_float2(__fadd_rn(p.x, cxv), __fadd_rn(p.y, cyv)) : p;
+          }
+        }
+      }
+    }
+    __syncthreads();
   }
-  const float2 c = corr[i];
-  q[i] = make_float2(p.x + c.x, p.y + c.y);
+}
+
+size_t correct_smem() {
+  return sizeof(SmemNet) + (size_t)kFuseThreads * kRow * 4 + kFuseThreads * 4;
 }
 
 // target = q - p (the first K-1 iterations' correction)
@@ -578,28 +724,45 @@ __global__ void k_target(uint32_t n, const float2* __restrict__ pos, const float
   target[i] = make_float2(v.x - p.x, v.y - p.y);
 }
 
-// Frame metrics of the gate: per taking-part particle the deepest overlap
-// with a neighbour of the 3x3 cells (min_d - distance, if positive), summed
-// and maxed; and the kinetic energy.  out[0] += sum of overlaps, out[1] =
-// max overlap (as float bits, non-negative so integer max works), out[2] +=
-// number of particles, out[3] += kinetic energy, out[4] += the kinetic
-// energy the plain frame would have.
+// Sums of a block: 5 values per thread (sum, max, sum, sum, sum order in
+// `v`), reduced over the block and written to part[blockIdx.x * 8 + k].
+__device__ __forceinline__ void block_partials(float (&v)[5], float* __restrict__ part) {
+  __shared__ float red[32][5];
+#pragma unroll
+  for (uint32_t o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const float u = __shfl_xor_sync(0xffffffffu, v[k], o);
+      v[k] = k == 1 ? fmaxf(v[k], u) : v[k] + u;
+    }
+  }
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < 5; ++k) red[warp][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    float acc = red[0][threadIdx.x];
+    for (uint32_t w = 1; w < nw; ++w)
+      acc = threadIdx.x == 1 ? fmaxf(acc, red[w][threadIdx.x]) : acc + red[w][threadIdx.x];
+    part[blockIdx.x * 8 + threadIdx.x] = acc;
+  }
+}
+
+// Frame metrics (report only): per taking-part particle the deepest overlap
+// with a taking-part neighbour of the 3x3 cells, max(0, max_j (min_d -
+// |p_j - p_i|)); per block: [0] sum of overlaps, [1] max overlap, [2] number
+// of taking-part particles, [3] kinetic energy, [4] 0.
 __global__ void __launch_bounds__(256)
 k_penetration(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32_t n,
               const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ cell_of,
               const float2* __restrict__ pos, const float2* __restrict__ vel,
-              const float2* __restrict__ vel_before, float* __restrict__ out) {
+              float* __restrict__ part) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  float pen = 0.f, ke = 0.f, cnt = 0.f, ke_plain = 0.f;
+  float pen = 0.f, ke = 0.f, cnt = 0.f;
   if (i < n) {
     const float2 v = vel[i];
-    ke = 0.5f * (v.x * v.x + v.y * v.y);
-    // the plain frame's kinetic energy: its velocity changes only through
-    // gravity, the clamp and wall reflections (which keep |v|)
-    const float2 u = vel_before[i];
-    const float ux = fminf(fmaxf(u.x, -ph.vmax), ph.vmax);
-    const float uy = fminf(fmaxf(u.y - ph.gravity, -ph.vmax), ph.vmax);
-    ke_plain = 0.5f * (ux * ux + uy * uy);
+    ke = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y)));
     const uint32_t c = cell_of[i];
     if (i - cell_start[c] < ph.cap) {
       cnt = 1.f;
@@ -617,29 +780,75 @@ k_penetration(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint
           for (uint32_t j = js; j < je; ++j) {
             if (j == i) continue;
             const float2 pj = pos[j];
-            const float dx = pj.x - pi.x, dy = pj.y - pi.y;
-            const float d = sqrtf(dx * dx + dy * dy);
-            pen = fmaxf(pen, ph.min_d - d);
+            const float dx = __fsub_rn(pj.x, pi.x), dy = __fsub_rn(pj.y, pi.y);
+            const float s2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+            if (s2 >= ph.skip_d2) continue;  // no overlap
+            pen = fmaxf(pen, __fsub_rn(ph.min_d, __fsqrt_rn(s2)));
           }
         }
       }
     }
   }
-  float s = pen, k = ke, m = pen, nc = cnt, kp = ke_plain;
+  float v[5] = {pen, pen, cnt, ke, 0.f};
+  block_partials(v, part);
+}
+
+// Deterministic sum of per-block partials: out[k] for k in 0..4 (out[1] the
+// max), one block of 256 threads.
+__global__ void __launch_bounds__(256)
+k_reduce_partials(const float* __restrict__ part, uint32_t nparts, float* __restrict__ out) {
+  float v[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (uint32_t b = threadIdx.x; b < nparts; b += blockDim.x) {
 #pragma unroll
-  for (uint32_t o = 1; o < 32; o <<= 1) {
-    s += __shfl_xor_sync(0xffffffffu, s, o);
-    k += __shfl_xor_sync(0xffffffffu, k, o);
-    kp += __shfl_xor_sync(0xffffffffu, kp, o);
-    nc += __shfl_xor_sync(0xffffffffu, nc, o);
-    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    for (int k = 0; k < 5; ++k) v[k] = k == 1 ? fmaxf(v[k], part[b * 8 + k]) : v[k] + part[b * 8 + k];
   }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&out[0], s);
-    atomicMax(reinterpret_cast<int*>(&out[1]), __float_as_int(m));
-    atomicAdd(&out[2], nc);
-    atomicAdd(&out[3], k);
-    atomicAdd(&out[4], kp);
+  block_partials(v, out - blockIdx.x * 8);
+}
+
+// The fallback gate of a surrogate frame, one block.  The partials come from
+// the final Jacobi iteration ([0] sum and [1] max of the deepest overlap
+// before that iteration, [2] taking-part count, [3] kinetic energy of the
+// output, [4] kinetic energy the plain frame has); `mode`:
+//   0  after the surrogate correction and the last plain iteration: the frame
+//      falls back when its mean overlap exceeds the latest plain frame's by
+//      more than `tol`, or its kinetic energy deviates from the plain value
+//      by more than `max_drift` (relative); NaN falls back too;
+//   1  after the (gated) fallback solve: when the frame fell back, its plain
+//      metrics become the reference;
+//   2  after a plain calibration frame: its metrics become the reference.
+__global__ void __launch_bounds__(256)
+k_gate(const float* __restrict__ part, uint32_t nparts, GateState* __restrict__ gs, int mode) {
+  if (mode == 1 && gs->fallback == 0u) return;
+  float v[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (uint32_t b = threadIdx.x; b < nparts; b += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) v[k] = k == 1 ? fmaxf(v[k], part[b * 8 + k]) : v[k] + part[b * 8 + k];
+  }
+  __shared__ float tot[8];
+  block_partials(v, tot - blockIdx.x * 8);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const float mean = tot[2] > 0.f ? tot[0] / tot[2] : 0.f;
+  const float drift = tot[4] > 0.f ? fabsf(tot[3] - tot[4]) / tot[4] : 0.f;
+  if (mode == 0) {
+    const bool ok = mean <= gs->pen_ref + gs->tol && drift <= gs->max_drift;
+    gs->fallback = ok ? 0u : 1u;
+    gs->frames += 1;
+    gs->drift_max = fmaxf(gs->drift_max, drift);
+    if (ok) {
+      gs->pen_sum += mean;
+      gs->pen_max = fmaxf(gs->pen_max, tot[1]);
+    } else {
+      gs->fallbacks += 1;
+    }
+  } else {
+    gs->pen_ref = mean;
+    gs->pen_sum += mean;
+    gs->pen_max = fmaxf(gs->pen_max, tot[1]);
+    if (mode == 2) {
+      gs->frames += 1;
+      gs->calibrations += 1;
+    }
   }
 }
 
@@ -687,6 +896,25 @@ cudaError_t launch_knn_features(const SolveArgs& a, uint16_t* x, cudaStream_t st
   return cudaGetLastError();
 }
 
+cudaError_t launch_surrogate_correct(const MlpDev& m, const SolveArgs& a, float2* q, float2* corr,
+                                     int blocks, cudaStream_t st) {
+  if (a.n == 0) return cudaSuccess;
+  const size_t smem = correct_smem();
+  cudaError_t e = cudaFuncSetAttribute(k_surrogate_correct,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int need = (int)((a.n + kFuseThreads - 1) / kFuseThreads);
+  k_surrogate_correct<<<need < blocks ? need : blocks, kFuseThreads, smem, st>>>(
+      m, a.worlds, a.nworlds, a.ph, a.n, a.cell_start, a.cell_of, a.pos, a.vel, q, corr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gate(const float* part, uint32_t nparts, GateState* gs, int mode,
+                        cudaStream_t st) {
+  k_gate<<<1, 256, 0, st>>>(part, nparts, gs, mode);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_mlp_forward(const MlpDev& m, const uint16_t* x, uint32_t n, float2* y,
                                int blocks, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
@@ -718,14 +946,6 @@ cudaError_t launch_adam(const MlpDev& m, const float* grad, float* mom1, float* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_apply_correction(const SolveArgs& a, const float2* corr, float2* q,
-                                    cudaStream_t st) {
-  if (a.n == 0) return cudaSuccess;
-  k_apply_correction<<<(a.n + 255) / 256, 256, 0, st>>>(a.worlds, a.ph, a.n, a.cell_start,
-                                                        a.cell_of, a.pos, corr, q);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_target(uint32_t n, const float2* pos, const float2* q, float2* target,
                           cudaStream_t st) {
   if (n == 0) return cudaSuccess;
@@ -734,10 +954,15 @@ cudaError_t launch_target(uint32_t n, const float2* pos, const float2* q, float2
 }
 
 cudaError_t launch_penetration(const SolveArgs& a, const float2* pos, const float2* vel,
-                               float* out, cudaStream_t st) {
-  if (a.n == 0) return cudaSuccess;
-  k_penetration<<<(a.n + 255) / 256, 256, 0, st>>>(a.worlds, a.nworlds, a.ph, a.n, a.cell_start,
-                                                   a.cell_of, pos, vel, a.vel, out);
+                               float* part, float* out, cudaStream_t st) {
+  const uint32_t blocks = (a.n + 255) / 256;
+  if (blocks) {
+    k_penetration<<<blocks, 256, 0, st>>>(a.worlds, a.nworlds, a.ph, a.n, a.cell_start, a.cell_of,
+                                          pos, vel, part);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  k_reduce_partials<<<1, 256, 0, st>>>(part, blocks, out);
   return cudaGetLastError();
 }
 

@@ -124,14 +124,20 @@ __device__ __forceinline__ void enforce_limits(const WorldDev& w, float vmax,
 // the host); since sqrt_rn is monotonic, s >= skip_d2 is exactly the
 // reference's `distance > MIN_DISTANCE`, decided without the square root.
 __device__ __forceinline__ bool push_factor(float ex, float ey, float min_d,
-                                            float skip_d2, float& f) {
+                                            float skip_d2, float& f, float& dist) {
   const float s = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
   if (s >= skip_d2) return false;
   float d = __fsqrt_rn(s);
+  dist = d;
   if (d > min_d) return false;
   if (d == 0.0f) d = 0.0001f;
   f = __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(min_d, d)), d);
   return true;
+}
+__device__ __forceinline__ bool push_factor(float ex, float ey, float min_d,
+                                            float skip_d2, float& f) {
+  float d;
+  return push_factor(ex, ey, min_d, skip_d2, f, d);
 }
 
 __device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {

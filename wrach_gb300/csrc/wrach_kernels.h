@@ -23,6 +23,8 @@ struct SolveArgs {
   uint32_t* keys;               // next cell of each output particle
   Ctrl* ctrl;
   uint32_t block;               // threads per block of the solve kernels (<= 512)
+  const uint32_t* run_if;       // extended solve: skip the launch when *run_if == 0 (optional)
+  float* part;                  // final extended pass: per-block metrics, 8 floats a block (optional)
 };
 
 cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st);
@@ -110,7 +112,29 @@ struct MlpDev {
   uint16_t* w3t;           // BF16 [8][in]
 };
 
+// Device-side state of the surrogate's fallback gate (k_gate).
+struct GateState {
+  float tol;          // allowed excess of the mean overlap over the reference (px)
+  float max_drift;    // allowed relative kinetic-energy deviation
+  float pen_ref;      // mean overlap before the last iteration, latest plain frame
+  uint32_t fallback;  // the current frame falls back to the plain solve
+  uint32_t frames, fallbacks, calibrations;
+  float pen_sum, pen_max, drift_max;
+  uint32_t pad[6];
+};
+
 cudaError_t launch_knn_features(const SolveArgs& a, uint16_t* x, cudaStream_t st);
+// Fused surrogate correction of the binned frame: q = p + network(features)
+// for taking-part particles; `corr` optional.
+cudaError_t launch_surrogate_correct(const MlpDev& m, const SolveArgs& a, float2* q, float2* corr,
+                                     int blocks, cudaStream_t st);
+cudaError_t launch_gate(const float* part, uint32_t nparts, GateState* gs, int mode,
+                        cudaStream_t st);
+// Number of blocks (and so of partials) of an extended solve launch.
+inline uint32_t solve_blocks(const SolveArgs& a) {
+  const uint32_t threads = a.block ? a.block : 256;
+  return (a.n + threads - 1) / threads;
+}
 cudaError_t launch_mlp_forward(const MlpDev& m, const uint16_t* x, uint32_t n, float2* y,
                                int blocks, cudaStream_t st);
 cudaError_t launch_mlp_backward(const MlpDev& m, const uint16_t* x, const float2* target,
@@ -118,14 +142,14 @@ cudaError_t launch_mlp_backward(const MlpDev& m, const uint16_t* x, const float2
                                 int blocks, cudaStream_t st);
 cudaError_t launch_adam(const MlpDev& m, const float* grad, float* mom1, float* mom2, float lr,
                         uint32_t step, cudaStream_t st);
-cudaError_t launch_apply_correction(const SolveArgs& a, const float2* corr, float2* q,
-                                    cudaStream_t st);
 cudaError_t launch_target(uint32_t n, const float2* pos, const float2* q, float2* target,
                           cudaStream_t st);
 cudaError_t launch_errors(const SolveArgs& a, const float2* corr, const float2* target, float* out,
                           cudaStream_t st);
+// Report-only frame metrics: per-block partials into `part` (8 floats per
+// 256 particles), their sums into out[0..4].
 cudaError_t launch_penetration(const SolveArgs& a, const float2* pos, const float2* vel,
-                               float* out, cudaStream_t st);
+                               float* part, float* out, cudaStream_t st);
 
 // Headless point rasteriser (render.cu): `cover` holds width_px * height_px
 // u32 scratch, `image` the 8-bit result.
