@@ -207,6 +207,10 @@ def launch_bytes(kind, n, c):
     return 0
 
 
+# the launches of the rebin (a stable counting sort), in order
+REBIN_STEPS = ["count", "scan", "scatter", "place", "large_cells"]
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -271,8 +275,9 @@ def run_ours(args):
               "frames_%d_%d_ms" % (len(traj) - 99, len(traj)): float(traj[-100:].mean())}
 
     # per-kernel durations of eager frames sampled along the trajectory
-    kinds = (["jacobi"] * (cfg["iterations"] - 1) + ["jacobi_final"] if cfg["mode"] else
-             ["solve_reference"]) + ["rebin"]
+    solve_kinds = (["jacobi"] * (cfg["iterations"] - 1) + ["jacobi_final"] if cfg["mode"] else
+                   ["solve_reference"])
+    kinds = solve_kinds + ["rebin_" + s for s in REBIN_STEPS]
     sim.set_particles(pos, vel)
     every = max(1, args.trajectory // max(1, args.profile_frames))
     prof, nprof = np.zeros(len(kinds)), 0
@@ -285,8 +290,10 @@ def run_ours(args):
             sim.step(1)
     prof /= max(nprof, 1)
     per_kind = {}
-    for k, ms in zip(kinds, prof):
+    for k, ms in zip(solve_kinds, prof):
         per_kind.setdefault(k, []).append(ms)
+    rebin_steps = {s: float(ms) for s, ms in zip(REBIN_STEPS, prof[len(solve_kinds):])}
+    per_kind["rebin"] = [float(sum(rebin_steps.values()))]
     dom = max(per_kind, key=lambda k: sum(per_kind[k]))
     dom_ms = statistics.mean(per_kind[dom])
     peak, peak_kind = measured_peak()
@@ -344,6 +351,7 @@ def run_ours(args):
                           "achieved": step_bytes / (max_ms / args.steps / 1000.0) / 1e9,
                           "frac": step_bytes / (max_ms / args.steps / 1000.0) / 1e9 / peak},
         "kernels": kernels,
+        "rebin_steps_ms": rebin_steps,
         "trajectory": dict(phases, frames=args.trajectory,
                            note="frames of one pass; late frames are the collapsed floor"),
         "gpu_launches": launches,

@@ -74,7 +74,8 @@ typedef struct WrachConfig {
                               default 9 */
   uint32_t capacity;       /* 0 = max_particles_per_frame of the grid */
   int32_t device;          /* CUDA ordinal (default 0) */
-  uint32_t rebin_blocks;   /* blocks of the rebin kernel, 0 = all that fit */
+  uint32_t rebin_blocks;   /* blocks of the radix-sort rebin (allocation-free
+                              packing), 0 = all that fit */
   uint32_t solve_block;    /* threads per block of the solve kernels, a
                               multiple of 32 up to 512, 0 = 256 */
   uint32_t reserved[5];
@@ -191,17 +192,20 @@ typedef struct WrachStats {
   uint32_t flags;             /* sticky WRACH_FLAG_* bits */
   uint32_t frames;            /* frames stepped since create */
   uint32_t overflow;          /* particles without destination room */
-  uint32_t rebin_blocks;      /* co-resident blocks of the rebin kernel */
+  uint32_t rebin_blocks;      /* co-resident blocks of the radix-sort rebin */
   uint32_t tiles;             /* tiles of the cell table */
   uint32_t particles;         /* particles in the frame, all worlds */
   uint32_t cells;             /* grid cells, all worlds */
-  uint32_t reserved[9];
+  uint32_t huge_cells;        /* cells of more than 2048 particles the rebin
+                                 sorted in global memory, since create */
+  uint32_t reserved[8];
 } WrachStats;
 
 /* Reads the counters; blocks. */
 int wrach_stats(WrachContext *ctx, WrachStats *out);
 
-/* Phase trace of the latest rebin launch: %globaltimer (ns) at each phase
+/* Phase trace of the latest radix-sort rebin (wrach_pack_noalloc's; frames
+ * and uploads use the counting sort): %globaltimer (ns) at each phase
  * boundary, as recorded by its first block; *count receives the number of
  * entries (at most 32).  Blocks.  No counterpart in the reference. */
 int wrach_rebin_trace(WrachContext *ctx, uint64_t *ns, uint32_t cap,

@@ -72,7 +72,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("flags", ctypes.c_uint32), ("frames", ctypes.c_uint32),
                 ("overflow", ctypes.c_uint32), ("rebin_blocks", ctypes.c_uint32),
                 ("tiles", ctypes.c_uint32), ("particles", ctypes.c_uint32),
-                ("cells", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 9)]
+                ("cells", ctypes.c_uint32), ("huge_cells", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 8)]
 
 
 class SurrogateStats(ctypes.Structure):

@@ -6,8 +6,9 @@ assets/shaders/prefix_sum.wgsl:9-15) and lists changing them as a TODO
 (README.md:28).  Here the launch shape is a per-context setting, and `tune`
 picks it by timing candidates on the workload itself:
 
-  rebin_blocks   co-resident blocks of the rebin kernel (its grid barriers
-                 get cheaper with fewer blocks, its phases faster with more)
+  rebin_blocks   co-resident blocks of the rebin's radix-sort fallback (it
+                 runs only for cells beyond 8192 particles, so it is tuned
+                 only when candidates are passed)
   solve_block    threads per block of the solve kernels
   cell_size      only when the caller allows it: it changes which particles
                  share a cell, hence the capacity rule and the summation order
@@ -108,8 +109,7 @@ def tune(config, positions, velocities, worlds=None, frames=10, rebin_blocks=Non
     if use_cache and key in cache:
         return dataclasses.replace(config, **cache[key]["choice"]), cache[key]["ms"]
     if rebin_blocks is None:
-        sms = max(1, max_blocks // 3)
-        rebin_blocks = sorted({b for b in (sms, 2 * sms, max_blocks) if b <= max_blocks})
+        rebin_blocks = (max_blocks,)
     timings = {}
     best, best_ms = None, float("inf")
     for cs in cell_sizes:

@@ -105,6 +105,10 @@ struct WrachContext {
   uint32_t* hist = nullptr;
   uint32_t* tile_sums = nullptr;  // one word per tile of the cell table
   uint32_t ntiles = 0;
+  unsigned long long* scan_status = nullptr;  // counting sort: look-back words
+  uint32_t* big_list = nullptr;               // counting sort: large-cell work list
+  uint32_t big_cap = 0;
+  int sms = 0;
   uint32_t key_bits = 0, digit_bits = 0;
   Ctrl* ctrl = nullptr;
   int rebin_grid = 0;
@@ -189,7 +193,7 @@ void release(WrachContext* ctx) {
   void* ptrs[] = {ctx->worlds_d, ctx->pos, ctx->vel, ctx->pos_o, ctx->vel_o,
                   ctx->q1, ctx->q2, ctx->cell_of[0], ctx->cell_of[1],
                   ctx->cs[0], ctx->cs[1], ctx->keys, ctx->kA, ctx->kB,
-                  ctx->iA, ctx->iB, ctx->hist, ctx->tile_sums, ctx->ctrl,
+                  ctx->iA, ctx->iB, ctx->hist, ctx->tile_sums, ctx->ctrl, ctx->scan_status, ctx->big_list,
                   ctx->stage_pos, ctx->stage_vel, ctx->table_tmp, ctx->counts, ctx->render_cover, ctx->render_image,
                   ctx->gather_idx, ctx->gather_out};
   for (void* p : ptrs) dfree(p);
@@ -222,6 +226,11 @@ int ensure_sort_capacity(WrachContext* ctx, size_t need) {
     *b = nullptr;
   }
   for (auto b : bufs) CK(dalloc(b, cap));
+  dfree(ctx->big_list);
+  ctx->big_list = nullptr;
+  // at most cap / (kSmallCell + 1) cells can be larger than kSmallCell
+  ctx->big_cap = (uint32_t)(cap / (wrach::kSmallCell + 1) + 2);
+  CK(dalloc(&ctx->big_list, ctx->big_cap));
   ctx->sort_cap = cap;
   drop_graphs(ctx);
   return WRACH_OK;
@@ -294,6 +303,13 @@ wrach::RebinArgs rebin_args(WrachContext* ctx) {
   r.keys = ctx->keys;
   r.counts = ctx->counts;
   r.ctrl = ctx->ctrl;
+  r.ticket = ctx->kA;
+  r.idx_tmp = ctx->iA;
+  r.cell_tmp = ctx->kB;
+  r.idx_alt = ctx->iB;
+  r.status = ctx->scan_status;
+  r.big_list = ctx->big_list;
+  r.big_cap = ctx->big_cap;
   return r;
 }
 
@@ -339,16 +355,20 @@ int enqueue_frame(WrachContext* ctx) {
   r.vel_dst = ctx->vel;
   r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
   r.force_general = 0;
-  CK(wrach::launch_rebin(r, ctx->rebin_grid, st));
-  mark(ctx);
-  ctx->launches += 1;
+  for (int step = 0; step < wrach::kCountSortSteps; ++step) {
+    bool launched;
+    CK(wrach::launch_count_sort_step(r, step, ctx->sms, st, &launched));
+    if (launched) mark(ctx);
+  }
+  ctx->launches += wrach::count_sort_launches(r.n);
   ctx->cur ^= 1;
   return WRACH_OK;
 }
 
 uint32_t frame_launches(const WrachContext* ctx) {
-  if (ctx->ph.mode == WRACH_MODE_REFERENCE) return 2;
-  return std::max<uint32_t>(ctx->ph.iterations, 1) + 1;
+  const uint32_t rebin = wrach::count_sort_launches(ctx->n);
+  if (ctx->ph.mode == WRACH_MODE_REFERENCE) return 1 + rebin;
+  return std::max<uint32_t>(ctx->ph.iterations, 1) + rebin;
 }
 
 // One frame captured as a CUDA graph, instantiated once per table parity
@@ -530,6 +550,10 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   // one sum per tile of kTileCells cells of the table
   ctx->ntiles = (ctx->ncells + wrach::kTileCells - 1) / wrach::kTileCells;
   if ((e = dalloc(&ctx->tile_sums, ctx->ntiles)) != cudaSuccess) return oom(e);
+  if ((e = dalloc(&ctx->scan_status, (size_t)ctx->ncells / wrach::kCountScanTile + 1)) != cudaSuccess)
+    return oom(e);
+  if ((e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device)) != cudaSuccess)
+    return oom(e);
   if ((e = dalloc(&ctx->ctrl, 1)) != cudaSuccess) return oom(e);
   if ((e = cudaMemset(ctx->ctrl, 0, sizeof(Ctrl))) != cudaSuccess) return oom(e);
   if ((e = dalloc(&ctx->table_tmp, (size_t)ctx->max_world_cells + 2)) != cudaSuccess) return oom(e);
@@ -603,8 +627,8 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
   r.vel_dst = ctx->vel_o;
   r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
   r.force_general = 1;
-  CK(wrach::launch_rebin(r, ctx->rebin_grid, ctx->stream));
-  ctx->launches += 1;
+  CK(wrach::launch_count_sort(r, ctx->sms, ctx->stream));
+  ctx->launches += wrach::count_sort_launches(r.n);
 
   // per-world counts from the new table
   const uint32_t nw = ctx->nworlds;
@@ -950,8 +974,8 @@ int enqueue_rebin(WrachContext* ctx) {
   r.vel_dst = ctx->vel;
   r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
   r.force_general = 0;
-  CK(wrach::launch_rebin(r, ctx->rebin_grid, ctx->stream));
-  ctx->launches += 1;
+  CK(wrach::launch_count_sort(r, ctx->sms, ctx->stream));
+  ctx->launches += wrach::count_sort_launches(r.n);
   ctx->cur ^= 1;
   return WRACH_OK;
 }
@@ -1239,6 +1263,7 @@ int wrach_stats(WrachContext* ctx, WrachStats* out) {
   out->tiles = ctx->ntiles;
   out->particles = ctx->n;
   out->cells = ctx->ncells;
+  out->huge_cells = h.huge_cells;
   return WRACH_OK;
 }
 

@@ -48,7 +48,10 @@ struct Ctrl {
   uint32_t bar_gen;     // grid barrier generation
   uint32_t overflow;    // particles dropped for lack of destination room
   uint32_t frames;      // rebin launches that were frames (not uploads)
-  uint32_t pad[9];
+  uint32_t scan_ticket; // counting sort: tiles of the cell scan claimed so far
+  uint32_t big_count;   // counting sort: cells on the large-cell work list
+  uint32_t huge_cells;  // counting sort: cells sorted in global memory, since create
+  uint32_t pad[6];
   // %globaltimer at the phase boundaries of the latest rebin launch, taken
   // by block 0 (phase trace; kPhaseSlots entries, unused ones zero)
   uint64_t phase_ns[32];

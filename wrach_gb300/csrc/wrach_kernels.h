@@ -58,6 +58,14 @@ struct RebinArgs {
   int force_general;            // set for uploads (not counted as frames)
   uint32_t* counts;             // ncells + 1 zeros on entry and on exit
   Ctrl* ctrl;
+  // the counting sort (count_sort.cu); unused by the radix sort
+  uint32_t* ticket;             // n: slot of each particle inside its cell (arrival order)
+  uint32_t* idx_tmp;            // n: source index per slot, arrival order
+  uint32_t* cell_tmp;           // n: cell per slot
+  unsigned long long* status;   // ceil(ncells / kCountScanTile): look-back words of the scan
+  uint32_t* idx_alt;            // n: scratch of the in-memory sort of very large cells
+  uint32_t* big_list;           // big_cap: cells of more than kSmallCell particles
+  uint32_t big_cap;
 };
 
 constexpr uint32_t kRebinThreads = 256;
@@ -73,6 +81,22 @@ size_t rebin_dynamic_smem(uint32_t digit_bits);
 // Blocks the cooperative rebin kernel launches with on `device`.
 int rebin_grid_size(int device, uint32_t digit_bits);
 cudaError_t launch_rebin(const RebinArgs& a, int grid, cudaStream_t st);
+
+// The same rebin as a stable counting sort over the cells (count_sort.cu),
+// five plain launches: cells of up to kSmallCell particles are ranked per
+// slot, cells of up to kBigCell in shared memory, larger ones in global
+// memory by one block each.
+constexpr uint32_t kCountScanTile = 8192;
+constexpr uint32_t kSmallCell = 64;
+constexpr uint32_t kBigCell = 2048;
+cudaError_t launch_count_sort(const RebinArgs& a, int sms, cudaStream_t st);
+// The same, one step at a time (steps 0 .. kCountSortSteps - 1: count, scan,
+// scatter, place, large cells); *launched is false for a step that has
+// nothing to do.
+constexpr int kCountSortSteps = 5;
+cudaError_t launch_count_sort_step(const RebinArgs& a, int step, int sms, cudaStream_t st,
+                                   bool* launched);
+uint32_t count_sort_launches(uint32_t n);
 
 // Keys for an upload re-pack: the first n_keep sources are particles of the
 // current frame (their cell, or `ncells` if they belong to world `target`),
