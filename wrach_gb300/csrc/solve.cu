@@ -91,15 +91,31 @@ k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
 // take part in the pushes, as pushed particles and as neighbours; the rest of
 // an over-full cell keep their position.  The neighbour order is fixed (3x3
 // cells in row-major order, table order inside a cell), so the sum is
-// deterministic.  FINAL fuses gravity, integration, boundaries, the velocity
-// clamp and the key emission.  METRICS (final pass only) also writes the
-// block's sums for the surrogate's fallback gate to part[blockIdx.x * 8 +
-// k]: [0] sum and [1] max over taking-part particles of the deepest overlap
-// max(0, min_d - distance) with a pushing neighbour (measured on the pass's
-// input), [2] the number of taking-part particles, [3] the kinetic energy of
-// the output and [4] the kinetic energy a plain frame gives (gravity, the
-// clamp and wall reflections only change the velocity).  A launch whose
-// `run_if` flag reads 0 returns at once.
+// deterministic.
+//
+// Per neighbour row, two passes: pass 1 marks the candidates within reach
+// with an exact squared-distance test (cheap, every lane), pass 2 applies
+// the reference's push (IEEE square root and division) to those only, in
+// candidate order.  A row whose cells are all within capacity is one
+// contiguous range of candidates and is scanned in one loop.
+//
+// FINAL fuses gravity, integration, boundaries, the velocity clamp and the
+// key emission.  METRICS (final pass only) also writes the block's sums for
+// the surrogate's fallback gate to part[blockIdx.x * 8 + k]: [0] sum and [1]
+// max over taking-part particles of the deepest overlap max(0, min_d -
+// distance) with a pushing neighbour (measured on the pass's input), [2] the
+// number of taking-part particles, [3] the kinetic energy of the output and
+// [4] the kinetic energy a plain frame gives (gravity, the clamp and wall
+// reflections only change the velocity).  A launch whose `run_if` flag reads
+// 0 returns at once.
+// Candidate index of mask bit b of a neighbour row: contiguous rows map bit
+// b to s0 + b; rows with an over-full cell keep 16 bits per cell.
+__device__ __forceinline__ uint32_t row_candidate(bool merged, uint32_t s0, uint32_t s1,
+                                                  uint32_t s2, uint32_t b) {
+  if (merged) return s0 + b;
+  return (b < 16 ? s0 : (b < 32 ? s1 - 16 : s2 - 32)) + b;
+}
+
 template <bool FINAL, bool METRICS>
 __global__ void __launch_bounds__(512)
 k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
@@ -110,16 +126,20 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
          const uint32_t* __restrict__ run_if, float* __restrict__ part) {
   static_assert(FINAL || !METRICS, "metrics come from the final pass");
   if (run_if && *run_if == 0u) return;
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < n;
   uint32_t flags = 0;
   float pen = 0.f, taking = 0.f, ke = 0.f, ke_plain = 0.f;
-  if (i < n) {
+  WorldDev w;
+  float2 qi = make_float2(0.f, 0.f);
+  float ax = 0.0f, ay = 0.0f;
+  if (live) {
     const uint32_t c = cell_of[i];
-    const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
+    w = worlds[world_of_cell(worlds, nworlds, c)];
     uint32_t cx, cy;
     cell_xy(w, c - w.cell_off, cx, cy);
-    const float2 qi = qin[i];
-    float ax = 0.0f, ay = 0.0f;
+    qi = qin[i];
     if (do_push && i - cell_start[c] < ph.cap) {
       if (METRICS) taking = 1.f;
       // the table entries of the three neighbour rows first: independent
@@ -137,44 +157,68 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
           st[r][k] = (row_ok && x0 + k <= x1 + 1) ? cell_start[rb + k] : 0u;
       }
       const uint32_t ncol = x1 - x0 + 1;  // 2 or 3 cells per row
+      static_assert(kMaxCellCapacity <= 16, "16 mask bits per cell");
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
         // the row's taking-part candidates: up to three cells of at most
-        // `cap` particles each, at most 3 * kMaxCellCapacity <= 48 of them
+        // `cap` particles each; a NaN distance counts as within reach, as in
+        // the reference's test
         const uint32_t s0 = st[r][0], s1 = st[r][1], s2 = st[r][2], s3 = st[r][3];
         const uint32_t e0 = min(s1, s0 + ph.cap);
         const uint32_t e1 = min(s2, s1 + ph.cap);
         const uint32_t e2 = ncol == 3 ? min(s3, s2 + ph.cap) : s2;
-        // pass 1: which candidates are within reach (cheap, every lane); a
-        // NaN distance counts as within reach, as in the reference's test
-        static_assert(kMaxCellCapacity <= 16, "16 mask bits per cell");
         uint64_t close = 0;
-        uint32_t k = 0;
-        for (uint32_t j = s0; j < e0; ++j, ++k) {
-          const float2 qj = qin[j];
-          const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
-          if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
-            close |= 1ull << k;
-        }
-        k = 16;
-        for (uint32_t j = s1; j < e1; ++j, ++k) {
-          const float2 qj = qin[j];
-          const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
-          if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
-            close |= 1ull << k;
-        }
-        k = 32;
-        for (uint32_t j = s2; j < e2; ++j, ++k) {
-          const float2 qj = qin[j];
-          const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
-          if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
-            close |= 1ull << k;
+        const bool merged = e0 == s1 && (ncol == 2 || e1 == s2);
+        if (merged) {
+          // no over-full cell before the last: one contiguous range, two
+          // candidates per step
+          const uint32_t e = ncol == 3 ? e2 : e1;
+          uint32_t j = s0;
+          for (; j + 1 < e; j += 2) {
+            const float2 qa = qin[j], qb = qin[j + 1];
+            const float ax0 = __fsub_rn(qa.x, qi.x), ay0 = __fsub_rn(qa.y, qi.y);
+            const float bx0 = __fsub_rn(qb.x, qi.x), by0 = __fsub_rn(qb.y, qi.y);
+            const bool ca = !(__fadd_rn(__fmul_rn(ax0, ax0), __fmul_rn(ay0, ay0)) >= ph.skip_d2);
+            const bool cb = !(__fadd_rn(__fmul_rn(bx0, bx0), __fmul_rn(by0, by0)) >= ph.skip_d2);
+            close |= (uint64_t)((ca ? 1u : 0u) | (cb ? 2u : 0u)) << (j - s0);
+          }
+          if (j < e) {
+            const float2 qa = qin[j];
+            const float ax0 = __fsub_rn(qa.x, qi.x), ay0 = __fsub_rn(qa.y, qi.y);
+            if (!(__fadd_rn(__fmul_rn(ax0, ax0), __fmul_rn(ay0, ay0)) >= ph.skip_d2))
+              close |= 1ull << (j - s0);
+          }
+          // the particle itself is not its own neighbour
+          if (i >= s0 && i < e) close &= ~(1ull << (i - s0));
+        } else {
+          uint32_t k = 0;
+          for (uint32_t j = s0; j < e0; ++j, ++k) {
+            const float2 qj = qin[j];
+            const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
+            if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
+              close |= 1ull << k;
+          }
+          k = 16;
+          for (uint32_t j = s1; j < e1; ++j, ++k) {
+            const float2 qj = qin[j];
+            const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
+            if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
+              close |= 1ull << k;
+          }
+          k = 32;
+          for (uint32_t j = s2; j < e2; ++j, ++k) {
+            const float2 qj = qin[j];
+            const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
+            if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
+              close |= 1ull << k;
+          }
         }
         // pass 2: the reference's push for those, in candidate order
+        // (cell.rs:79-95)
         while (close) {
           const uint32_t b = __ffsll((long long)close) - 1;
           close &= close - 1;
-          const uint32_t j = (b < 16 ? s0 : (b < 32 ? s1 - 16 : s2 - 32)) + b;
+          const uint32_t j = row_candidate(merged, s0, s1, s2, b);
           const float2 qj = qin[j];
           const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
           float f, d;
@@ -185,6 +229,8 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
         }
       }
     }
+  }
+  if (live) {
     const float qx = __fsub_rn(qi.x, ax), qy = __fsub_rn(qi.y, ay);
     if (!FINAL) {
       qout[i] = make_float2(qx, qy);
@@ -217,7 +263,6 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
         v[k] = k == 1 ? fmaxf(v[k], u) : __fadd_rn(v[k], u);
       }
     }
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0)
 #pragma unroll
       for (int k = 0; k < 5; ++k) red[warp][k] = v[k];
@@ -225,8 +270,8 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
     if (threadIdx.x < 5) {
       const uint32_t nw = (blockDim.x + 31) >> 5;
       float acc = red[0][threadIdx.x];
-      for (uint32_t w = 1; w < nw; ++w)
-        acc = threadIdx.x == 1 ? fmaxf(acc, red[w][threadIdx.x]) : __fadd_rn(acc, red[w][threadIdx.x]);
+      for (uint32_t wi = 1; wi < nw; ++wi)
+        acc = threadIdx.x == 1 ? fmaxf(acc, red[wi][threadIdx.x]) : __fadd_rn(acc, red[wi][threadIdx.x]);
       part[blockIdx.x * 8 + threadIdx.x] = acc;
     }
   }
