@@ -10,8 +10,9 @@
 //   cell_of[2]        cell of each binned particle (u32)
 //   cs[2]             cell-start table, cells + 1 u32 (ping-pong per frame)
 //   keys              next cell of each solve output (u32)
-//   kA kB iA iB hist  general re-sort scratch
-//   status            look-back words, one per tile of kTileCells cells
+//   kA kB iA iB       rebin scratch (tickets, slot cells, slot sources, sort ping-pong)
+//   tile_sums         rebin: particles per tile of 2048 cells (zero between frames)
+//   hist              radix-sort scratch (wrach_pack_noalloc's sort)
 //   ctrl              counters and sticky flags
 #include <algorithm>
 #include <cmath>
@@ -105,7 +106,6 @@ struct WrachContext {
   uint32_t* hist = nullptr;
   uint32_t* tile_sums = nullptr;  // one word per tile of the cell table
   uint32_t ntiles = 0;
-  unsigned long long* scan_status = nullptr;  // counting sort: look-back words
   uint32_t* big_list = nullptr;               // counting sort: large-cell work list
   uint32_t big_cap = 0;
   int sms = 0;
@@ -193,7 +193,7 @@ void release(WrachContext* ctx) {
   void* ptrs[] = {ctx->worlds_d, ctx->pos, ctx->vel, ctx->pos_o, ctx->vel_o,
                   ctx->q1, ctx->q2, ctx->cell_of[0], ctx->cell_of[1],
                   ctx->cs[0], ctx->cs[1], ctx->keys, ctx->kA, ctx->kB,
-                  ctx->iA, ctx->iB, ctx->hist, ctx->tile_sums, ctx->ctrl, ctx->scan_status, ctx->big_list,
+                  ctx->iA, ctx->iB, ctx->hist, ctx->tile_sums, ctx->ctrl, ctx->big_list,
                   ctx->stage_pos, ctx->stage_vel, ctx->table_tmp, ctx->counts, ctx->render_cover, ctx->render_image,
                   ctx->gather_idx, ctx->gather_out};
   for (void* p : ptrs) dfree(p);
@@ -307,7 +307,6 @@ wrach::RebinArgs rebin_args(WrachContext* ctx) {
   r.idx_tmp = ctx->iA;
   r.cell_tmp = ctx->kB;
   r.idx_alt = ctx->iB;
-  r.status = ctx->scan_status;
   r.big_list = ctx->big_list;
   r.big_cap = ctx->big_cap;
   return r;
@@ -327,9 +326,13 @@ int enqueue_frame(WrachContext* ctx) {
     mark(ctx);
     ctx->launches += 1;
   } else {
+    // the last pass takes the rebin's tickets (it computes the keys)
+    wrach::SolveArgs fin = a;
+    fin.count = wrach::CountDev{ctx->counts, ctx->tile_sums, ctx->kA, ctx->ncells,
+                                wrach::kCountScanShift};
     const uint32_t K = ctx->ph.iterations;
     if (K == 0) {
-      CK(wrach::launch_solve_extended(a, ctx->pos, ctx->pos_o, true, 0, st));
+      CK(wrach::launch_solve_extended(fin, ctx->pos, ctx->pos_o, true, 0, st));
       mark(ctx);
       ctx->launches += 1;
     } else {
@@ -340,11 +343,12 @@ int enqueue_frame(WrachContext* ctx) {
         mark(ctx);
         src = dst;
       }
-      CK(wrach::launch_solve_extended(a, src, ctx->pos_o, true, 1, st));
+      CK(wrach::launch_solve_extended(fin, src, ctx->pos_o, true, 1, st));
       mark(ctx);
       ctx->launches += K;
     }
   }
+  const bool tickets_taken = ctx->ph.mode != WRACH_MODE_REFERENCE;
   wrach::RebinArgs r = rebin_args(ctx);
   r.n = ctx->n;
   r.dst_capacity = ctx->total_cap;
@@ -355,12 +359,12 @@ int enqueue_frame(WrachContext* ctx) {
   r.vel_dst = ctx->vel;
   r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
   r.force_general = 0;
-  for (int step = 0; step < wrach::kCountSortSteps; ++step) {
+  for (int step = tickets_taken ? 1 : 0; step < wrach::kCountSortSteps; ++step) {
     bool launched;
     CK(wrach::launch_count_sort_step(r, step, ctx->sms, st, &launched));
     if (launched) mark(ctx);
   }
-  ctx->launches += wrach::count_sort_launches(r.n);
+  ctx->launches += wrach::count_sort_launches(r.n) - (tickets_taken && r.n ? 1 : 0);
   ctx->cur ^= 1;
   return WRACH_OK;
 }
@@ -368,7 +372,7 @@ int enqueue_frame(WrachContext* ctx) {
 uint32_t frame_launches(const WrachContext* ctx) {
   const uint32_t rebin = wrach::count_sort_launches(ctx->n);
   if (ctx->ph.mode == WRACH_MODE_REFERENCE) return 1 + rebin;
-  return std::max<uint32_t>(ctx->ph.iterations, 1) + rebin;
+  return std::max<uint32_t>(ctx->ph.iterations, 1) + rebin - (ctx->n ? 1 : 0);
 }
 
 // One frame captured as a CUDA graph, instantiated once per table parity
@@ -550,8 +554,9 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   // one sum per tile of kTileCells cells of the table
   ctx->ntiles = (ctx->ncells + wrach::kTileCells - 1) / wrach::kTileCells;
   if ((e = dalloc(&ctx->tile_sums, ctx->ntiles)) != cudaSuccess) return oom(e);
-  if ((e = dalloc(&ctx->scan_status, (size_t)ctx->ncells / wrach::kCountScanTile + 1)) != cudaSuccess)
-    return oom(e);
+  // the counting sort's tile sums reuse the table tile sums (kTileCells <= 2048)
+  static_assert(wrach::kTileCells <= wrach::kCountScanTile, "tile sums buffer large enough");
+  if ((e = cudaMemset(ctx->tile_sums, 0, (size_t)ctx->ntiles * 4)) != cudaSuccess) return oom(e);
   if ((e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device)) != cudaSuccess)
     return oom(e);
   if ((e = dalloc(&ctx->ctrl, 1)) != cudaSuccess) return oom(e);

@@ -6,11 +6,14 @@
 //   count    per warp, the particles of one cell (__match_any_sync) take one
 //            atomic on the cell's counter; each particle's ticket (its slot
 //            inside the cell, arrival order) is the returned base plus its
-//            rank among the warp's particles of that cell
-//   scan     exclusive scan of the per-cell counts in tiles of 8192 cells,
-//            tiles claimed in launch order and chained by a decoupled
-//            look-back in which the whole block reads 256 predecessors at a
-//            time; it writes the cell-start table and clears the counts
+//            rank among the warp's particles of that cell; per warp one more
+//            atomic adds the particles of each tile of 2048 cells to the
+//            tile's sum.  A frame of the extended physics takes the tickets
+//            in its last Jacobi pass instead (the keys are computed there)
+//   scan     exclusive scan of the per-cell counts, one block per tile of
+//            2048 cells; a tile's prefix is the sum of the earlier tiles'
+//            sums (already final, so no block waits); it writes the
+//            cell-start table and clears the counts
 //   scatter  source index and cell of every particle to table start + ticket
 //            (arrival order inside a cell)
 //   place    the stable order: inside a cell, a particle's rank is the number
@@ -33,36 +36,20 @@ namespace wrach {
 
 namespace {
 
-constexpr uint32_t kScanThreads = 256, kScanPer = 32;
+constexpr uint32_t kScanThreads = 256, kScanPer = 8;
 constexpr uint32_t kScanTile = kScanThreads * kScanPer;
-static_assert(kScanTile == kCountScanTile, "tile size shared with the buffer sizing");
-constexpr uint32_t kFlagAggregate = 1u, kFlagInclusive = 2u;
+static_assert(kScanTile == kCountScanTile, "tile size shared with the tickets' tile sums");
 
-__device__ __forceinline__ unsigned long long status_word(uint32_t flag, uint32_t value) {
-  return ((unsigned long long)flag << 32) | value;
-}
-
-__global__ void __launch_bounds__(256) k_cs_count(RebinArgs a, uint32_t nstatus) {
+__global__ void __launch_bounds__(256) k_cs_count(RebinArgs a) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t lane = threadIdx.x & 31;
-  if (i == 0) {
-    a.ctrl->scan_ticket = 0u;
-    a.ctrl->big_count = 0u;
-    if (!a.force_general) a.ctrl->frames += 1;
-  }
-  for (uint32_t t = i; t < nstatus; t += stride) a.status[t] = 0ull;
   // whole warps walk the particles, so every lane takes part in the match
   for (uint32_t base = i - lane; base < a.n; base += stride) {
     const uint32_t j = base + lane;
     const uint32_t k = j < a.n ? a.keys[j] : a.ncells;
-    const uint32_t peers = __match_any_sync(0xffffffffu, k);
-    const uint32_t leader = __ffs(peers) - 1;
-    uint32_t first = 0;
-    if (lane == leader && k < a.ncells) first = atomicAdd(&a.counts[k], __popc(peers));
-    first = __shfl_sync(0xffffffffu, first, leader);
-    if (j < a.n)
-      a.ticket[j] = k < a.ncells ? first + __popc(peers & ((1u << lane) - 1u)) : 0xFFFFFFFFu;
+    const uint32_t t = warp_ticket(k, a.ncells, a.counts, a.tile_sums, kCountScanShift);
+    if (j < a.n) a.ticket[j] = t;
   }
 }
 
@@ -78,19 +65,19 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red) {
   return s;
 }
 
+// One block per tile of 2048 cells.  The tile's prefix is the sum of the
+// earlier tiles' counts, which the tickets' pass has already totalled, so no
+// block waits for another.
 __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
-  __shared__ uint32_t s_tile, s_flags;
   __shared__ uint32_t warp_sum[kScanThreads / 32], red[kScanThreads / 32];
   const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  if (t == 0) {
-    s_tile = atomicAdd(&a.ctrl->scan_ticket, 1u);
-    s_flags = 0u;
+  const uint32_t tile = blockIdx.x, n = a.ncells;
+  if (tile == 0 && t == 0) {
+    a.ctrl->big_count = 0u;
+    if (!a.force_general) a.ctrl->frames += 1;
   }
-  __syncthreads();
-  const uint32_t tile = s_tile, n = a.ncells;
   const uint32_t c0 = tile * kScanTile + t * kScanPer;
   uint32_t v[kScanPer];
-  uint32_t sum = 0;
   if (c0 + kScanPer <= n) {
     const uint4* src = reinterpret_cast<const uint4*>(a.counts + c0);
 #pragma unroll
@@ -102,8 +89,13 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
 #pragma unroll
     for (uint32_t u = 0; u < kScanPer; ++u) v[u] = c0 + u < n ? __ldcg(a.counts + c0 + u) : 0u;
   }
+  uint32_t sum = 0;
 #pragma unroll
   for (uint32_t u = 0; u < kScanPer; ++u) sum += v[u];
+  // the earlier tiles' total
+  uint32_t pre = 0;
+  for (uint32_t u = t; u < tile; u += kScanThreads) pre += __ldcg(a.tile_sums + u);
+  const uint32_t prefix = block_sum(pre, red);
   // block-wide exclusive scan of the per-thread sums
   uint32_t x = sum;
 #pragma unroll
@@ -119,51 +111,7 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
     before += w < warp ? warp_sum[w] : 0u;
     total += warp_sum[w];
   }
-  const uint32_t excl = before + x - sum;
-  // the tile's prefix: publish the aggregate, look back 256 tiles at a time,
-  // publish the inclusive value
-  unsigned long long* st = a.status;
-  if (t == 0)
-    st_release_u64(reinterpret_cast<uint64_t*>(st + tile),
-                   status_word(tile == 0 ? kFlagInclusive : kFlagAggregate, total));
-  uint32_t prefix = 0;
-  if (tile > 0) {
-    int base = (int)tile - 1;
-    const uint64_t t0 = global_ns();
-    bool timed_out = false;
-    while (true) {
-      const int p = base - (int)t;
-      unsigned long long w = p >= 0 ? ld_acquire_u64(reinterpret_cast<const uint64_t*>(st + p))
-                                    : status_word(kFlagInclusive, 0u);
-      uint32_t flag = (uint32_t)(w >> 32);
-      if (__syncthreads_or(flag == 0u)) {
-        // a predecessor has not published yet: wait (bounded; thread 0's
-        // clock decides for the block)
-        if (t == 0 && global_ns() - t0 > kWaitLimitNs) s_flags = kFlagTimeout;
-        __syncthreads();
-        timed_out = s_flags != 0u;
-        if (!timed_out) {
-          __nanosleep(64);
-          continue;
-        }
-      }
-      // the nearest inclusive predecessor in the window, then the sum of the
-      // values up to it
-      __shared__ uint32_t s_near;
-      if (t == 0) s_near = kScanThreads;
-      __syncthreads();
-      if (flag == kFlagInclusive) atomicMin(&s_near, t);
-      __syncthreads();
-      const uint32_t near = s_near;
-      prefix += block_sum(t <= near ? (uint32_t)w : 0u, red);
-      if (near < kScanThreads || timed_out) break;
-      base -= (int)kScanThreads;
-    }
-    if (t == 0)
-      st_release_u64(reinterpret_cast<uint64_t*>(st + tile),
-                     status_word(kFlagInclusive, prefix + total));
-  }
-  uint32_t run = prefix + excl;
+  uint32_t run = prefix + before + x - sum;
   if (c0 + kScanPer <= n) {
     uint4* dst = reinterpret_cast<uint4*>(a.cs_new + c0);
     uint4* cnt = reinterpret_cast<uint4*>(a.counts + c0);
@@ -187,14 +135,13 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
       run += v[u];
     }
   }
-  if (t == 0) {
-    if ((tile + 1) * kScanTile >= n) a.cs_new[n] = prefix + total;
-    if (s_flags) atomicOr(&a.ctrl->flags, s_flags);
-  }
+  if (t == 0 && (tile + 1) * kScanTile >= n) a.cs_new[n] = prefix + total;
 }
 
-__global__ void __launch_bounds__(256) k_cs_scatter(RebinArgs a) {
+__global__ void __launch_bounds__(256) k_cs_scatter(RebinArgs a, uint32_t ntiles) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  // the scan has read the tile sums: clear them for the next rebin
+  for (uint32_t u = i; u < ntiles; u += gridDim.x * blockDim.x) a.tile_sums[u] = 0u;
   if (i >= a.n) return;
   const uint32_t k = a.keys[i];
   if (k >= a.ncells) return;
@@ -359,14 +306,18 @@ cudaError_t launch_count_sort_step(const RebinArgs& a, int step, int sms, cudaSt
   const uint32_t nblk = (a.n + 255) / 256;
   *launched = true;
   if (step == 0) {
-    k_cs_count<<<nblk ? nblk : 1u, 256, 0, st>>>(a, ntiles);
+    if (!nblk) {
+      *launched = false;
+      return cudaSuccess;
+    }
+    k_cs_count<<<nblk, 256, 0, st>>>(a);
   } else if (step == 1) {
     k_cs_scan<<<ntiles ? ntiles : 1u, kScanThreads, 0, st>>>(a);
   } else if (!nblk) {
     *launched = false;
     return cudaSuccess;
   } else if (step == 2) {
-    k_cs_scatter<<<nblk, 256, 0, st>>>(a);
+    k_cs_scatter<<<nblk, 256, 0, st>>>(a, ntiles);
   } else if (step == 3) {
     k_cs_place<<<nblk, 256, 0, st>>>(a);
   } else {
@@ -384,6 +335,6 @@ cudaError_t launch_count_sort(const RebinArgs& a, int sms, cudaStream_t st) {
   return cudaSuccess;
 }
 
-uint32_t count_sort_launches(uint32_t n) { return n ? 5u : 2u; }
+uint32_t count_sort_launches(uint32_t n) { return n ? 5u : 1u; }
 
 }  // namespace wrach

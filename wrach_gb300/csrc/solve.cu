@@ -123,7 +123,7 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
          const uint32_t* __restrict__ cell_of, const float2* __restrict__ qin,
          float2* __restrict__ qout, const float2* __restrict__ vin,
          float2* __restrict__ vout, uint32_t* __restrict__ keys, Ctrl* ctrl,
-         const uint32_t* __restrict__ run_if, float* __restrict__ part) {
+         const uint32_t* __restrict__ run_if, float* __restrict__ part, CountDev count) {
   static_assert(FINAL || !METRICS, "metrics come from the final pass");
   if (run_if && *run_if == 0u) return;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -134,6 +134,7 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
   WorldDev w;
   float2 qi = make_float2(0.f, 0.f);
   float ax = 0.0f, ay = 0.0f;
+  uint32_t key = count.ncells;  // no cell, unless the final pass computes one
   if (live) {
     const uint32_t c = cell_of[i];
     w = worlds[world_of_cell(worlds, nworlds, c)];
@@ -241,7 +242,8 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
       enforce_limits(w, ph.vmax, px, py, ux, uy);
       qout[i] = make_float2(px, py);
       vout[i] = make_float2(ux, uy);
-      keys[i] = next_key(w, px, py, flags);
+      key = next_key(w, px, py, flags);
+      keys[i] = key;
       if (METRICS) {
         ke = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)));
         const float cx = fminf(fmaxf(v.x, -ph.vmax), ph.vmax);
@@ -249,6 +251,12 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
         ke_plain = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
       }
     }
+  }
+  if (FINAL && count.ticket) {
+    // the rebin's tickets (every lane of the warp takes part)
+    const uint32_t t = warp_ticket(key, count.ncells, count.counts, count.tile_sums,
+                                   count.tile_shift);
+    if (live) count.ticket[i] = t;
   }
   if (FINAL) publish_flags(ctrl, flags);
   if (METRICS) {
@@ -298,15 +306,15 @@ cudaError_t launch_solve_extended(const SolveArgs& a, const float2* qin,
   if (final_pass && a.part)
     k_jacobi<true, true><<<blocks, threads, 0, st>>>(
         a.worlds, a.nworlds, a.ph, a.n, do_push, a.cell_start, a.cell_of, qin,
-        qout, a.vel, a.vel_out, a.keys, a.ctrl, a.run_if, a.part);
+        qout, a.vel, a.vel_out, a.keys, a.ctrl, a.run_if, a.part, a.count);
   else if (final_pass)
     k_jacobi<true, false><<<blocks, threads, 0, st>>>(
         a.worlds, a.nworlds, a.ph, a.n, do_push, a.cell_start, a.cell_of, qin,
-        qout, a.vel, a.vel_out, a.keys, a.ctrl, a.run_if, nullptr);
+        qout, a.vel, a.vel_out, a.keys, a.ctrl, a.run_if, nullptr, a.count);
   else
     k_jacobi<false, false><<<blocks, threads, 0, st>>>(
         a.worlds, a.nworlds, a.ph, a.n, do_push, a.cell_start, a.cell_of, qin,
-        qout, nullptr, nullptr, nullptr, a.ctrl, a.run_if, nullptr);
+        qout, nullptr, nullptr, nullptr, a.ctrl, a.run_if, nullptr, CountDev{});
   return cudaGetLastError();
 }
 

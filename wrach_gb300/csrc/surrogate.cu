@@ -898,13 +898,22 @@ cudaError_t launch_knn_features(const SolveArgs& a, uint16_t* x, cudaStream_t st
 
 cudaError_t launch_surrogate_correct(const MlpDev& m, const SolveArgs& a, float2* q, float2* corr,
                                      int blocks, cudaStream_t st) {
+  (void)blocks;
   if (a.n == 0) return cudaSuccess;
   const size_t smem = correct_smem();
   cudaError_t e = cudaFuncSetAttribute(k_surrogate_correct,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  // persistent: one wave of co-resident blocks
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_surrogate_correct, kFuseThreads,
+                                                         smem)) != cudaSuccess)
+    return e;
+  const int grid = sms * (per_sm > 0 ? per_sm : 1);
   const int need = (int)((a.n + kFuseThreads - 1) / kFuseThreads);
-  k_surrogate_correct<<<need < blocks ? need : blocks, kFuseThreads, smem, st>>>(
+  k_surrogate_correct<<<need < grid ? need : grid, kFuseThreads, smem, st>>>(
       m, a.worlds, a.nworlds, a.ph, a.n, a.cell_start, a.cell_of, a.pos, a.vel, q, corr);
   return cudaGetLastError();
 }

@@ -48,7 +48,7 @@ struct Ctrl {
   uint32_t bar_gen;     // grid barrier generation
   uint32_t overflow;    // particles dropped for lack of destination room
   uint32_t frames;      // rebin launches that were frames (not uploads)
-  uint32_t scan_ticket; // counting sort: tiles of the cell scan claimed so far
+  uint32_t unused0;
   uint32_t big_count;   // counting sort: cells on the large-cell work list
   uint32_t huge_cells;  // counting sort: cells sorted in global memory, since create
   uint32_t pad[6];
@@ -142,6 +142,43 @@ __device__ __forceinline__ bool push_factor(float ex, float ey, float min_d,
   float d;
   return push_factor(ex, ey, min_d, skip_d2, f, d);
 }
+
+// Counting-sort ticket of a particle whose next cell is k (k >= ncells: no
+// cell).  All 32 lanes of the warp call it together.  Per warp, one atomic
+// per cell present gives each particle its slot inside the cell (arrival
+// order, lane order inside the warp), and one atomic per tile of
+// 2^tile_shift cells adds the tile's particle count.  Returns the slot, or
+// 0xFFFFFFFF for no cell.
+__device__ __forceinline__ uint32_t warp_ticket(uint32_t k, uint32_t ncells, uint32_t* counts,
+                                                uint32_t* tile_sums, uint32_t tile_shift) {
+  const uint32_t lane = threadIdx.x & 31;
+  const bool valid = k < ncells;
+  const uint32_t peers = __match_any_sync(0xffffffffu, valid ? k : 0xFFFFFFFFu);
+  const uint32_t leader = __ffs(peers) - 1;
+  uint32_t first = 0;
+  if (lane == leader && valid) first = atomicAdd(&counts[k], __popc(peers));
+  first = __shfl_sync(0xffffffffu, first, leader);
+  const uint32_t tile = valid ? k >> tile_shift : 0xFFFFFFFFu;
+  const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+  const uint32_t t0 = __shfl_sync(0xffffffffu, tile, vmask ? __ffs(vmask) - 1 : 0);
+  if (__all_sync(0xffffffffu, !valid || tile == t0)) {
+    // the common case: the warp's particles fall in one tile
+    if (lane == 0 && vmask) atomicAdd(&tile_sums[t0], __popc(vmask));
+  } else {
+    const uint32_t tpeers = __match_any_sync(0xffffffffu, tile);
+    if (valid && lane == (uint32_t)(__ffs(tpeers) - 1)) atomicAdd(&tile_sums[tile], __popc(tpeers));
+  }
+  return valid ? first + __popc(peers & ((1u << lane) - 1u)) : 0xFFFFFFFFu;
+}
+
+// What the last Jacobi pass needs to take the counting sort's tickets.
+struct CountDev {
+  uint32_t* counts;     // ncells, zero on entry
+  uint32_t* tile_sums;  // one per tile of 2^tile_shift cells, zero on entry
+  uint32_t* ticket;     // n; nullptr: no tickets
+  uint32_t ncells;
+  uint32_t tile_shift;
+};
 
 __device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
   uint64_t v;

@@ -25,6 +25,7 @@ struct SolveArgs {
   uint32_t block;               // threads per block of the solve kernels (<= 512)
   const uint32_t* run_if;       // extended solve: skip the launch when *run_if == 0 (optional)
   float* part;                  // final extended pass: per-block metrics, 8 floats a block (optional)
+  CountDev count;               // final extended pass: take the rebin's tickets (count.ticket set)
 };
 
 cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st);
@@ -62,7 +63,6 @@ struct RebinArgs {
   uint32_t* ticket;             // n: slot of each particle inside its cell (arrival order)
   uint32_t* idx_tmp;            // n: source index per slot, arrival order
   uint32_t* cell_tmp;           // n: cell per slot
-  unsigned long long* status;   // ceil(ncells / kCountScanTile): look-back words of the scan
   uint32_t* idx_alt;            // n: scratch of the in-memory sort of very large cells
   uint32_t* big_list;           // big_cap: cells of more than kSmallCell particles
   uint32_t big_cap;
@@ -86,13 +86,15 @@ cudaError_t launch_rebin(const RebinArgs& a, int grid, cudaStream_t st);
 // five plain launches: cells of up to kSmallCell particles are ranked per
 // slot, cells of up to kBigCell in shared memory, larger ones in global
 // memory by one block each.
-constexpr uint32_t kCountScanTile = 8192;
+constexpr uint32_t kCountScanShift = 11;
+constexpr uint32_t kCountScanTile = 1u << kCountScanShift;  // cells per scan tile (tile_sums entry)
 constexpr uint32_t kSmallCell = 64;
 constexpr uint32_t kBigCell = 2048;
 cudaError_t launch_count_sort(const RebinArgs& a, int sms, cudaStream_t st);
 // The same, one step at a time (steps 0 .. kCountSortSteps - 1: count, scan,
 // scatter, place, large cells); *launched is false for a step that has
-// nothing to do.
+// nothing to do.  Step 0 may be left out when the tickets were taken by the
+// last Jacobi pass (SolveArgs::count).
 constexpr int kCountSortSteps = 5;
 cudaError_t launch_count_sort_step(const RebinArgs& a, int step, int sms, cudaStream_t st,
                                    bool* launched);
