@@ -50,7 +50,7 @@ def parse():
     p.add_argument("--profile-frames", type=int, default=10)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
-    p.add_argument("--workload", default="lattice", choices=["lattice", "surrogate", "batch"],
+    p.add_argument("--workload", default="lattice", choices=["lattice", "surrogate", "batch", "viewport"],
                    help="lattice: the headline line; surrogate and batch print their own line")
     return p.parse_args()
 
@@ -493,6 +493,58 @@ def run_batch(args):
     return 0
 
 
+def run_viewport(args):
+    """Viewport streaming at the lattice-1M geometry: the 1,000,000 lattice
+    particles in the 1920x1080 viewport plus 1,000,000 more spread over the
+    3840x2160 area around it, in the world's store.  After 10 frames, each
+    timed move writes the frame back into the store (2 M particles
+    classified and compacted) and re-packs the frame under an anchor shifted
+    by 64 whole cells (and back), then runs one frame."""
+    import numpy as np
+    import torch
+    import wrach_gb300 as W
+    W.build()
+    dims, pos, vel, cfg, desc = workload()
+    rng = np.random.default_rng(1)
+    far = rng.uniform((-960.0, -540.0), (2880.0, 1620.0), size=(1_000_000, 2)).astype(np.float32)
+    far_vel = rng.normal(0, 1, size=far.shape).astype(np.float32)
+    cfg = dict(cfg, capacity=1_600_000)
+    sim = W.Simulation(W.WrachConfig(dimensions=dims, **cfg))
+    sim.add_particles(np.concatenate([pos, far]), np.concatenate([vel, far_vel]))
+    sim.step(10)
+    sim.sync()
+    moves = max(4, min(args.steps, 40))
+    anchors = [(64.0, 32.0), (0.0, 0.0)]
+    for k in range(2):  # warm-up: the store and staging buffers reach their size
+        sim.set_viewport(anchors[k % 2])
+        sim.step(1)
+    sim.sync()
+    stream = torch.cuda.ExternalStream(sim.stream)
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s0.record(stream)
+    frame_n = []
+    for k in range(moves):
+        sim.set_viewport(anchors[k % 2])
+        frame_n.append(sim.settings().particles_in_frame_count)
+        sim.step(1)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    store_n = len(sim.store()[0])
+    line = {"metric": "viewport moves/s (write-back + re-pack + 1 frame), 2M particles",
+            "value": moves / wall, "unit": "moves/s", "n_gpus": 1, "steps": moves,
+            "ms_per_step": 1000 * wall / moves, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "lattice-1M viewport streaming", "frame_particles": int(np.mean(frame_n)),
+                       "store_particles": store_n, "move_cells": [64, 32]},
+            "device_ms_per_step": s0.elapsed_time(s1) / moves,
+            "note": "host-timed: a move blocks (it reads the kept count and the per-world counts back)"}
+    sim.close()
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -501,6 +553,8 @@ def main():
         return run_surrogate(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "viewport":
+        return run_viewport(args)
     return run_ours(args)
 
 

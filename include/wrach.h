@@ -77,7 +77,7 @@ typedef struct WrachConfig {
   uint32_t rebin_blocks;   /* blocks of the radix-sort rebin (allocation-free
                               packing), 0 = all that fit */
   uint32_t solve_block;    /* threads per block of the solve kernels, a
-                              multiple of 32 up to 512, 0 = 256 */
+                              multiple of 32 up to 512, 0 = 128 */
   uint32_t reserved[5];
 } WrachConfig;
 
@@ -200,6 +200,36 @@ typedef struct WrachStats {
                                  sorted in global memory, since create */
   uint32_t reserved[8];
 } WrachStats;
+
+/* --- Viewport streaming ---------------------------------------------------
+ * Each world keeps a device-resident particle store, the counterpart of the
+ * reference's ParticleStore (runners/bevy/src/particle_store.rs:13-27):
+ * every particle added to the world, inside the viewport or not.  The frame
+ * is packed from the store's particles inside the viewport, as
+ * create_packed_data does (spatial_bin.rs:103-149); the others stay in the
+ * store, unsimulated.  Adding particles re-packs the world's frame from the
+ * store, as the reference does. */
+
+/* Writes the world's frame back into its store (the reference's TODO
+ * update_from_gpu, particle_store.rs:71-85): the store becomes its particles
+ * outside the viewport (store order) followed by the frame's particles (frame
+ * order).  Blocks.  No counterpart in the reference. */
+int wrach_write_back(WrachContext *ctx, uint32_t world);
+/* Moves the world's viewport to the same-size rectangle anchored at
+ * (anchor_x, anchor_y): writes the frame back, then packs the frame from the
+ * store under the new viewport (its walls move with it).  The grid size must
+ * stay the same (always so for a move by whole cells, or for a viewport whose
+ * sides are multiples of the cell size); otherwise
+ * WRACH_ERR_INVALID_ARGUMENT.  Blocks.  No counterpart in the reference. */
+int wrach_set_viewport(WrachContext *ctx, uint32_t world, float anchor_x,
+                       float anchor_y);
+/* Number of particles in the world's store. */
+int wrach_store_size(WrachContext *ctx, uint32_t world, uint32_t *count);
+/* Copies the world's store (positions, velocities as float pairs; either may
+ * be NULL) to host buffers of at least `capacity` >= store size entries.
+ * Blocks. */
+int wrach_read_store(WrachContext *ctx, uint32_t world, float *positions,
+                     float *velocities, uint32_t capacity);
 
 /* Reads the counters; blocks. */
 int wrach_stats(WrachContext *ctx, WrachStats *out);

@@ -185,3 +185,30 @@ def num_threads():
 
 def set_num_threads(n):
     lib().wo_set_num_threads(int(n))
+
+
+# -- viewport streaming (no reference implementation: the write-back is a TODO
+#    in runners/bevy/src/particle_store.rs:71-85; these are the rules the CUDA
+#    path states, restated here for its tests) --------------------------------
+
+def inside_viewport(w, pos):
+    """Mask of the particles whose cell (div_euclid, as create_packed_data:
+    spatial_bin.rs:48-64, 103-149) lies in the viewport's grid."""
+    pos = _f32(pos).reshape(-1, 2)
+    cs = int(w.cell_size)
+    blx, bly = cell_coord(w.view_anchor[0], cs), cell_coord(w.view_anchor[1], cs)
+    gx, gy = int(w.grid_dimensions[0]), int(w.grid_dimensions[1])
+    out = np.zeros(len(pos), bool)
+    for k, (x, y) in enumerate(pos):
+        cx, cy = cell_coord(float(x), cs) - blx, cell_coord(float(y), cs) - bly
+        out[k] = 0 <= cx < gx and 0 <= cy < gy
+    return out
+
+
+def write_back(w, store_pos, store_vel, frame_pos, frame_vel):
+    """The store after writing the frame back: its particles outside the
+    viewport (store order), then the frame's particles (frame order)."""
+    keep = ~inside_viewport(w, store_pos)
+    return (np.concatenate([_f32(store_pos).reshape(-1, 2)[keep], _f32(frame_pos).reshape(-1, 2)]),
+            np.concatenate([_f32(store_vel).reshape(-1, 2)[keep], _f32(frame_vel).reshape(-1, 2)]))
+

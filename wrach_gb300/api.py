@@ -271,6 +271,25 @@ class Simulation:
                                                   ctypes.byref(loss)))
         return float(loss.value)
 
+    # -- viewport streaming -------------------------------------------------
+    def write_back(self, world=0):
+        """Write the world's frame back into its store."""
+        self._check(self._L.wrach_write_back(self._ctx, world))
+
+    def set_viewport(self, anchor, world=0):
+        """Move the world's viewport to `anchor` (x, y), same size."""
+        self._check(self._L.wrach_set_viewport(self._ctx, world, float(anchor[0]), float(anchor[1])))
+
+    def store(self, world=0):
+        """(positions, velocities) of the world's store, (m, 2) float32 each."""
+        cnt = ctypes.c_uint32(0)
+        self._check(self._L.wrach_store_size(self._ctx, world, ctypes.byref(cnt)))
+        m = int(cnt.value)
+        pos = np.zeros((max(m, 1), 2), np.float32)
+        vel = np.zeros((max(m, 1), 2), np.float32)
+        self._check(self._L.wrach_read_store(self._ctx, world, _f32p(pos), _f32p(vel), max(m, 1)))
+        return pos[:m], vel[:m]
+
     def surrogate_correction(self, d_corr):
         """The fused kernel's correction of the current frame into the device
         buffer `d_corr` ((n, 2) float32)."""

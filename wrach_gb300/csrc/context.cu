@@ -115,6 +115,8 @@ struct WrachContext {
   std::vector<Store> stores;
   float2 *stage_pos = nullptr, *stage_vel = nullptr;
   size_t stage_cap = 0;
+  uint32_t* compact_sums = nullptr;   // viewport streaming: tile sums + 1 count word
+  size_t compact_cap = 0;
   uint32_t* counts = nullptr;     // per-cell counts of the rebin (ncells + 1)
   uint32_t* table_tmp = nullptr;  // one world's reference-layout table
   uint32_t* gather_idx = nullptr; // nworlds + 1
@@ -195,7 +197,7 @@ void release(WrachContext* ctx) {
                   ctx->cs[0], ctx->cs[1], ctx->keys, ctx->kA, ctx->kB,
                   ctx->iA, ctx->iB, ctx->hist, ctx->tile_sums, ctx->ctrl, ctx->big_list,
                   ctx->stage_pos, ctx->stage_vel, ctx->table_tmp, ctx->counts, ctx->render_cover, ctx->render_image,
-                  ctx->gather_idx, ctx->gather_out};
+                  ctx->gather_idx, ctx->gather_out, ctx->compact_sums};
   for (void* p : ptrs) dfree(p);
   for (auto& s : ctx->stores) {
     dfree(s.pos);
@@ -666,6 +668,57 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
   }
   drop_graphs(ctx);
   ctx->graph_ok = true;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return WRACH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Viewport streaming
+// ---------------------------------------------------------------------------
+
+// The world's store becomes: its particles outside the viewport (store
+// order), then the world's frame particles (frame order) -- per cell the
+// reference's write-back of the GPU's particles into its store
+// (particle_store.rs:71-85, a TODO there).
+int write_back_impl(WrachContext* ctx, uint32_t world) {
+  Store& s = ctx->stores[world];
+  const uint32_t nf = ctx->n_h[world], off = ctx->poff_h[world];
+  int rc;
+  if ((rc = ensure_sort_capacity(ctx, (size_t)s.n + 1))) return rc;
+  if ((rc = ensure_stage(ctx, (size_t)s.n + nf))) return rc;
+  const uint32_t ntiles = wrach::keep_outside_tiles(s.n);
+  if (ntiles + 1 > ctx->compact_cap) {
+    dfree(ctx->compact_sums);
+    ctx->compact_sums = nullptr;
+    ctx->compact_cap = 0;
+    CK(dalloc(&ctx->compact_sums, (size_t)ntiles + 1));
+    ctx->compact_cap = (size_t)ntiles + 1;
+  }
+  uint32_t kept = 0;
+  if (s.n) {
+    CK(wrach::launch_upload_keys(ctx->worlds_d, (int)ctx->nworlds, ctx->ncells, world, 0, nullptr,
+                                 s.n, s.pos, ctx->keys, ctx->stream));
+    CK(wrach::launch_keep_outside(ctx->keys, ctx->ncells, s.n, s.pos, s.vel, ctx->stage_pos,
+                                  ctx->stage_vel, ctx->compact_sums, ctx->compact_sums + ntiles,
+                                  ctx->stream));
+    ctx->launches += ntiles ? 4 : 2;
+    CK(cudaMemcpyAsync(&kept, ctx->compact_sums + ntiles, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  if (nf) {
+    CK(cudaMemcpyAsync(ctx->stage_pos + kept, ctx->pos + off, (size_t)nf * sizeof(float2),
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->stage_vel + kept, ctx->vel + off, (size_t)nf * sizeof(float2),
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  if ((rc = ensure_store(ctx, s, (size_t)kept + nf))) return rc;
+  if (kept + nf) {
+    CK(cudaMemcpyAsync(s.pos, ctx->stage_pos, ((size_t)kept + nf) * sizeof(float2),
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(s.vel, ctx->stage_vel, ((size_t)kept + nf) * sizeof(float2),
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  s.n = kept + nf;
   CK(cudaStreamSynchronize(ctx->stream));
   return WRACH_OK;
 }
@@ -1202,6 +1255,54 @@ int wrach_get_settings(WrachContext* ctx, uint32_t world, WrachWorldSettings* ou
   out->grid_dimensions[1] = w.gy;
   out->cell_size = w.cs;
   out->particles_in_frame_count = ctx->n_h[world];
+  return WRACH_OK;
+}
+
+int wrach_write_back(WrachContext* ctx, uint32_t world) {
+  if (!ctx) return WRACH_ERR_INVALID_ARGUMENT;
+  if (world >= ctx->nworlds) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "world out of range");
+  DeviceGuard guard(ctx->device);
+  return write_back_impl(ctx, world);
+}
+
+int wrach_set_viewport(WrachContext* ctx, uint32_t world, float anchor_x, float anchor_y) {
+  if (!ctx) return WRACH_ERR_INVALID_ARGUMENT;
+  if (world >= ctx->nworlds) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "world out of range");
+  DeviceGuard guard(ctx->device);
+  const WorldDev old = ctx->worlds_h[world];
+  WorldDev w;
+  if (world_settings_init(w, old.dim_x, old.dim_y, anchor_x, anchor_y, old.cs) || w.gx != old.gx ||
+      w.gy != old.gy)
+    return fail(ctx, WRACH_ERR_INVALID_ARGUMENT,
+                "the viewport at this anchor has a different grid size; move it by whole cells "
+                "or use a size that is a multiple of the cell size");
+  int rc = write_back_impl(ctx, world);
+  if (rc) return rc;
+  w.cell_off = old.cell_off;
+  ctx->worlds_h[world] = w;
+  CK(cudaMemcpyAsync(ctx->worlds_d + world, &ctx->worlds_h[world], sizeof(WorldDev),
+                     cudaMemcpyHostToDevice, ctx->stream));
+  // the frame, packed from the store under the new viewport
+  return upload_impl(ctx, world, nullptr, nullptr, 0, cudaMemcpyDeviceToDevice, false);
+}
+
+int wrach_store_size(WrachContext* ctx, uint32_t world, uint32_t* count) {
+  if (!ctx || !count || world >= ctx->nworlds) return WRACH_ERR_INVALID_ARGUMENT;
+  *count = ctx->stores[world].n;
+  return WRACH_OK;
+}
+
+int wrach_read_store(WrachContext* ctx, uint32_t world, float* positions, float* velocities,
+                     uint32_t capacity) {
+  if (!ctx || world >= ctx->nworlds) return WRACH_ERR_INVALID_ARGUMENT;
+  const Store& s = ctx->stores[world];
+  if (capacity < s.n) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "capacity smaller than the store");
+  DeviceGuard guard(ctx->device);
+  if (positions && s.n)
+    CK(cudaMemcpyAsync(positions, s.pos, (size_t)s.n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if (velocities && s.n)
+    CK(cudaMemcpyAsync(velocities, s.vel, (size_t)s.n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   return WRACH_OK;
 }
 

@@ -289,7 +289,7 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
 
 cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st) {
   if (a.ncells == 0) return cudaSuccess;
-  const uint32_t threads = a.block ? a.block : 256;
+  const uint32_t threads = a.block ? a.block : 128;
   const uint32_t blocks = (a.ncells + threads - 1) / threads;
   k_solve_reference<<<blocks, threads, 0, st>>>(
       a.worlds, a.nworlds, a.ph, a.ncells, a.cell_start, a.pos, a.vel,
@@ -301,7 +301,7 @@ cudaError_t launch_solve_extended(const SolveArgs& a, const float2* qin,
                                   float2* qout, bool final_pass, int do_push,
                                   cudaStream_t st) {
   if (a.n == 0) return cudaSuccess;
-  const uint32_t threads = a.block ? a.block : 256;
+  const uint32_t threads = a.block ? a.block : 128;
   const uint32_t blocks = (a.n + threads - 1) / threads;
   if (final_pass && a.part)
     k_jacobi<true, true><<<blocks, threads, 0, st>>>(

@@ -158,7 +158,7 @@ cudaError_t launch_gate(const float* part, uint32_t nparts, GateState* gs, int m
                         cudaStream_t st);
 // Number of blocks (and so of partials) of an extended solve launch.
 inline uint32_t solve_blocks(const SolveArgs& a) {
-  const uint32_t threads = a.block ? a.block : 256;
+  const uint32_t threads = a.block ? a.block : 128;
   return (a.n + threads - 1) / threads;
 }
 cudaError_t launch_mlp_forward(const MlpDev& m, const uint16_t* x, uint32_t n, float2* y,
@@ -176,6 +176,15 @@ cudaError_t launch_errors(const SolveArgs& a, const float2* corr, const float2* 
 // 256 particles), their sums into out[0..4].
 cudaError_t launch_penetration(const SolveArgs& a, const float2* pos, const float2* vel,
                                float* part, float* out, cudaStream_t st);
+
+// Viewport streaming (viewport.cu): the n items whose key is >= ncells
+// (outside the viewport), in order, into dst; *count receives how many.
+// `tile_sums` holds keep_outside_tiles(n) words of scratch.
+uint32_t keep_outside_tiles(uint32_t n);
+cudaError_t launch_keep_outside(const uint32_t* keys, uint32_t ncells, uint32_t n,
+                                const float2* pos, const float2* vel, float2* dst_pos,
+                                float2* dst_vel, uint32_t* tile_sums, uint32_t* count,
+                                cudaStream_t st);
 
 // Headless point rasteriser (render.cu): `cover` holds width_px * height_px
 // u32 scratch, `image` the 8-bit result.
