@@ -133,14 +133,18 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
   float pen = 0.f, taking = 0.f, ke = 0.f, ke_plain = 0.f;
   WorldDev w;
   float2 qi = make_float2(0.f, 0.f);
+  // the push sum, and the positions as packed pairs
   float ax = 0.0f, ay = 0.0f;
+  const f32x2* __restrict__ q64 = reinterpret_cast<const f32x2*>(qin);
+  f32x2 qi2 = 0ull;
   uint32_t key = count.ncells;  // no cell, unless the final pass computes one
   if (live) {
     const uint32_t c = cell_of[i];
     w = worlds[world_of_cell(worlds, nworlds, c)];
     uint32_t cx, cy;
     cell_xy(w, c - w.cell_off, cx, cy);
-    qi = qin[i];
+    qi2 = q64[i];
+    qi = make_float2(f2_x(qi2), f2_y(qi2));
     if (do_push && i - cell_start[c] < ph.cap) {
       if (METRICS) taking = 1.f;
       // the table entries of the three neighbour rows first: independent
@@ -176,42 +180,28 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
           const uint32_t e = ncol == 3 ? e2 : e1;
           uint32_t j = s0;
           for (; j + 1 < e; j += 2) {
-            const float2 qa = qin[j], qb = qin[j + 1];
-            const float ax0 = __fsub_rn(qa.x, qi.x), ay0 = __fsub_rn(qa.y, qi.y);
-            const float bx0 = __fsub_rn(qb.x, qi.x), by0 = __fsub_rn(qb.y, qi.y);
-            const bool ca = !(__fadd_rn(__fmul_rn(ax0, ax0), __fmul_rn(ay0, ay0)) >= ph.skip_d2);
-            const bool cb = !(__fadd_rn(__fmul_rn(bx0, bx0), __fmul_rn(by0, by0)) >= ph.skip_d2);
+            const f32x2 da = f2_sub(q64[j], qi2), db = f2_sub(q64[j + 1], qi2);
+            const bool ca = !(f2_len2(da) >= ph.skip_d2);
+            const bool cb = !(f2_len2(db) >= ph.skip_d2);
             close |= (uint64_t)((ca ? 1u : 0u) | (cb ? 2u : 0u)) << (j - s0);
           }
           if (j < e) {
-            const float2 qa = qin[j];
-            const float ax0 = __fsub_rn(qa.x, qi.x), ay0 = __fsub_rn(qa.y, qi.y);
-            if (!(__fadd_rn(__fmul_rn(ax0, ax0), __fmul_rn(ay0, ay0)) >= ph.skip_d2))
-              close |= 1ull << (j - s0);
+            if (!(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << (j - s0);
           }
           // the particle itself is not its own neighbour
           if (i >= s0 && i < e) close &= ~(1ull << (i - s0));
         } else {
           uint32_t k = 0;
           for (uint32_t j = s0; j < e0; ++j, ++k) {
-            const float2 qj = qin[j];
-            const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
-            if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
-              close |= 1ull << k;
+            if (j != i && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
           }
           k = 16;
           for (uint32_t j = s1; j < e1; ++j, ++k) {
-            const float2 qj = qin[j];
-            const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
-            if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
-              close |= 1ull << k;
+            if (j != i && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
           }
           k = 32;
           for (uint32_t j = s2; j < e2; ++j, ++k) {
-            const float2 qj = qin[j];
-            const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
-            if (j != i && !(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)) >= ph.skip_d2))
-              close |= 1ull << k;
+            if (j != i && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
           }
         }
         // pass 2: the reference's push for those, in candidate order
@@ -220,13 +210,13 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
           const uint32_t b = __ffsll((long long)close) - 1;
           close &= close - 1;
           const uint32_t j = row_candidate(merged, s0, s1, s2, b);
-          const float2 qj = qin[j];
-          const float dx = __fsub_rn(qj.x, qi.x), dy = __fsub_rn(qj.y, qi.y);
+          const f32x2 dd = f2_sub(q64[j], qi2);
           float f, d;
-          if (!push_factor(dx, dy, ph.min_d, ph.skip_d2, f, d)) continue;
+          if (!push_factor(f2_x(dd), f2_y(dd), ph.min_d, ph.skip_d2, f, d)) continue;
           if (METRICS) pen = fmaxf(pen, __fsub_rn(ph.min_d, d));
-          ax = __fadd_rn(ax, __fmul_rn(dx, f));
-          ay = __fadd_rn(ay, __fmul_rn(dy, f));
+          // scalar: a paired multiply feeding a paired add may be fused
+          ax = __fadd_rn(ax, __fmul_rn(f2_x(dd), f));
+          ay = __fadd_rn(ay, __fmul_rn(f2_y(dd), f));
         }
       }
     }

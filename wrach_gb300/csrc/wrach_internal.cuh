@@ -180,6 +180,42 @@ struct CountDev {
   uint32_t tile_shift;
 };
 
+// Packed pairs of binary32 values (x in the low word, as float2 in memory)
+// and sm_100-family paired arithmetic: each half rounds to nearest even on
+// its own, exactly as two __fadd_rn / __fsub_rn / __fmul_rn do.  A paired
+// multiply whose result feeds a paired add can be fused into one rounding
+// by the compiler (measured on sm_103a despite the .rn modifiers), so chains
+// that must round twice use the scalar intrinsics, which are never fused;
+// f2_len2 (paired multiply, then a scalar add of the halves) measured exact.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_pack(float x, float y) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+  return r;
+}
+__device__ __forceinline__ float f2_x(f32x2 v) { return __uint_as_float((uint32_t)v); }
+__device__ __forceinline__ float f2_y(f32x2 v) { return __uint_as_float((uint32_t)(v >> 32)); }
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+// Squared length of a packed (dx, dy): fl(fl(dx*dx) + fl(dy*dy)).
+__device__ __forceinline__ float f2_len2(f32x2 d) {
+  const f32x2 q = f2_mul(d, d);
+  return __fadd_rn(f2_x(q), f2_y(q));
+}
+
 __device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
   uint64_t v;
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
