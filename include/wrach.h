@@ -13,8 +13,10 @@
  * own CUDA stream; wrach_read and wrach_sync block until it is done.
  *
  * Data layout (the reference's, runners/bevy/src/spatial_bin.rs:20-33):
- *   positions, velocities: `capacity` float pairs (x, y), in cell order,
- *     zero past particles_in_frame_count;
+ *   positions, velocities: `capacity` float pairs (x, y), in cell order;
+ *     wrach_read writes the first particles_in_frame_count of them and
+ *     leaves the rest as they were (the reference's readback returns
+ *     whatever its buffers hold there);
  *   indices: grid cells + 2 u32, indices[0] = 0, indices[c + 1] = first
  *     particle of cell c, indices[cells + 1] = particles_in_frame_count.
  */

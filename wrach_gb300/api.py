@@ -171,11 +171,13 @@ class Simulation:
 
     def read(self, world=0, out=None):
         """(positions, velocities, indices) of a world: capacity x 2 float32
-        arrays (zero past the frame's particles) and the cells + 2 table."""
+        arrays and the cells + 2 table.  The library writes the frame's
+        particles only: arrays allocated here are zero past them, `out`
+        arrays keep what they held there."""
         cap = self.capacity(world)
         if out is None:
-            pos = np.empty((cap, 2), np.float32)
-            vel = np.empty((cap, 2), np.float32)
+            pos = np.zeros((cap, 2), np.float32)
+            vel = np.zeros((cap, 2), np.float32)
             idx = np.empty(self.cells(world) + 2, np.uint32)
         else:
             pos, vel, idx = out

@@ -124,6 +124,7 @@ struct WrachContext {
   std::string err;
   uint64_t launches = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  uint32_t graph_n[2] = {0, 0};       // particle count each graph was captured with
   bool graph_ok = true;
   uint32_t* render_cover = nullptr;   // wrach_render scratch and image
   uint8_t* render_image = nullptr;
@@ -408,6 +409,7 @@ int build_graph(WrachContext* ctx) {
     return WRACH_OK;
   }
   ctx->graph[parity] = exec;
+  ctx->graph_n[parity] = ctx->n;
   return WRACH_OK;
 }
 
@@ -605,7 +607,9 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
   }
   s.n += n_add;
 
-  const uint32_t n_keep = ctx->n, n_new = s.n;
+  // the frame's particles of other worlds are kept; with one world they all
+  // belong to the world being re-packed from its store, so none are
+  const uint32_t n_keep = ctx->nworlds > 1 ? ctx->n : 0u, n_new = s.n;
   const size_t nsrc = (size_t)n_keep + n_new;
   if (nsrc > 0xFFFFFFF0ull) {
     s.n = old_n;
@@ -613,13 +617,19 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
   }
   if ((rc = ensure_stage(ctx, nsrc))) return rc;
   if ((rc = ensure_sort_capacity(ctx, nsrc))) return rc;
+  // the sort's source: [kept frame particles, store]; without kept
+  // particles the store itself
+  const float2* src_pos = s.pos;
+  const float2* src_vel = s.vel;
   if (n_keep) {
     CK(cudaMemcpyAsync(ctx->stage_pos, ctx->pos, n_keep * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->stage_vel, ctx->vel, n_keep * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
-  }
-  if (n_new) {
-    CK(cudaMemcpyAsync(ctx->stage_pos + n_keep, s.pos, n_new * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->stage_vel + n_keep, s.vel, n_new * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+    if (n_new) {
+      CK(cudaMemcpyAsync(ctx->stage_pos + n_keep, s.pos, n_new * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+      CK(cudaMemcpyAsync(ctx->stage_vel + n_keep, s.vel, n_new * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    src_pos = ctx->stage_pos;
+    src_vel = ctx->stage_vel;
   }
   CK(wrach::launch_upload_keys(ctx->worlds_d, (int)ctx->nworlds, ctx->ncells, world, n_keep,
                                ctx->cell_of[ctx->cur], n_new, s.pos, ctx->keys, ctx->stream));
@@ -627,8 +637,8 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
   wrach::RebinArgs r = rebin_args(ctx);
   r.n = (uint32_t)nsrc;
   r.dst_capacity = ctx->total_cap;
-  r.pos_src = ctx->stage_pos;
-  r.vel_src = ctx->stage_vel;
+  r.pos_src = src_pos;
+  r.vel_src = src_vel;
   r.cs_new = ctx->cs[ctx->cur ^ 1];
   r.pos_dst = ctx->pos_o;
   r.vel_dst = ctx->vel_o;
@@ -666,7 +676,6 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
     ctx->n_h[w] = starts[w + 1] - starts[w];
     ctx->poff_h[w] = starts[w];
   }
-  drop_graphs(ctx);
   ctx->graph_ok = true;
   CK(cudaStreamSynchronize(ctx->stream));
   return WRACH_OK;
@@ -1169,6 +1178,12 @@ int wrach_step(WrachContext* ctx, uint32_t nsteps) {
   if (!ctx) return WRACH_ERR_INVALID_ARGUMENT;
   DeviceGuard guard(ctx->device);
   for (uint32_t s = 0; s < nsteps; ++s) {
+    // a graph holds the particle count (grid sizes) it was captured with;
+    // buffer reallocations drop the graphs
+    if (ctx->graph[ctx->cur] && ctx->graph_n[ctx->cur] != ctx->n) {
+      cudaGraphExecDestroy(ctx->graph[ctx->cur]);
+      ctx->graph[ctx->cur] = nullptr;
+    }
     if (ctx->graph_ok && !ctx->graph[ctx->cur]) {
       int rc = build_graph(ctx);
       if (rc) return rc;
@@ -1232,8 +1247,6 @@ int wrach_read(WrachContext* ctx, uint32_t world, float* positions, float* veloc
   }
   CK(cudaStreamSynchronize(ctx->stream));
   if (indices && ctx->nworlds == 1) indices[0] = 0;
-  if (positions && capacity > n) std::memset(positions + 2 * (size_t)n, 0, (size_t)(capacity - n) * 8);
-  if (velocities && capacity > n) std::memset(velocities + 2 * (size_t)n, 0, (size_t)(capacity - n) * 8);
   return WRACH_OK;
 }
 
