@@ -243,6 +243,15 @@ int wrach_stats(WrachContext *ctx, WrachStats *out);
 int wrach_rebin_trace(WrachContext *ctx, uint64_t *ns, uint32_t cap,
                       uint32_t *count);
 
+/* Self-test of the device's bounded wait, the one every device-side wait of
+ * the library uses (grid barriers): a one-thread kernel waits on a device
+ * word that nothing sets for limit_us microseconds (at most 1,000,000),
+ * then reports *timed_out = 1 and how long it waited.  The context stays
+ * usable; its sticky flags are not touched.  Blocks.  No counterpart in the
+ * reference. */
+int wrach_selftest_wait(WrachContext *ctx, uint32_t limit_us,
+                        uint32_t *timed_out, uint32_t *waited_us);
+
 /* The last error message of the context ("" if none). */
 const char *wrach_last_error(WrachContext *ctx);
 

@@ -273,6 +273,14 @@ class Simulation:
                                                   ctypes.byref(loss)))
         return float(loss.value)
 
+    def selftest_wait(self, limit_us):
+        """(timed out, microseconds waited) of a bounded device wait on a word
+        that nothing sets."""
+        t, us = ctypes.c_uint32(0), ctypes.c_uint32(0)
+        self._check(self._L.wrach_selftest_wait(self._ctx, int(limit_us), ctypes.byref(t),
+                                                ctypes.byref(us)))
+        return bool(t.value), int(us.value)
+
     # -- viewport streaming -------------------------------------------------
     def write_back(self, world=0):
         """Write the world's frame back into its store."""

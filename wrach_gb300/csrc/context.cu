@@ -1299,6 +1299,22 @@ int wrach_set_viewport(WrachContext* ctx, uint32_t world, float anchor_x, float 
   return upload_impl(ctx, world, nullptr, nullptr, 0, cudaMemcpyDeviceToDevice, false);
 }
 
+int wrach_selftest_wait(WrachContext* ctx, uint32_t limit_us, uint32_t* timed_out,
+                        uint32_t* waited_us) {
+  if (!ctx || !timed_out || !waited_us) return WRACH_ERR_INVALID_ARGUMENT;
+  if (limit_us > 1000000u) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "limit above 1 s");
+  DeviceGuard guard(ctx->device);
+  CK(wrach::launch_wait_probe(&ctx->ctrl->never_set, 0u, (uint64_t)limit_us * 1000u,
+                              ctx->gather_out, ctx->stream));
+  ctx->launches += 1;
+  uint32_t h[2];
+  CK(cudaMemcpyAsync(h, ctx->gather_out, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *timed_out = h[0];
+  *waited_us = h[1];
+  return WRACH_OK;
+}
+
 int wrach_store_size(WrachContext* ctx, uint32_t world, uint32_t* count) {
   if (!ctx || !count || world >= ctx->nworlds) return WRACH_ERR_INVALID_ARGUMENT;
   *count = ctx->stores[world].n;

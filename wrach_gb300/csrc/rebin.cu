@@ -85,15 +85,8 @@ __device__ void grid_barrier(Ctrl* ctrl, uint32_t& flags) {
       atomicExch(&ctrl->bar_count, 0u);
       __threadfence();
       st_release_u32(&ctrl->bar_gen, gen + 1);
-    } else {
-      const uint64_t t0 = global_ns();
-      while (ld_acquire_u32(&ctrl->bar_gen) == gen) {
-        if (global_ns() - t0 > kWaitLimitNs) {
-          flags |= kFlagTimeout;
-          break;
-        }
-        __nanosleep(64);
-      }
+    } else if (!wait_while_equal(&ctrl->bar_gen, gen, kWaitLimitNs)) {
+      flags |= kFlagTimeout;
     }
     __threadfence();
   }
@@ -447,6 +440,26 @@ __global__ void k_world_table(const uint32_t* __restrict__ cell_start,
 }
 
 }  // namespace
+
+namespace {
+
+// The bounded wait on a word: out[0] = 1 if it gave up, out[1] = the
+// microseconds it waited.
+__global__ void k_wait_probe(const uint32_t* word, uint32_t value, uint64_t limit_ns,
+                             uint32_t* out) {
+  const uint64_t t0 = global_ns();
+  const bool changed = wait_while_equal(word, value, limit_ns);
+  out[0] = changed ? 0u : 1u;
+  out[1] = (uint32_t)((global_ns() - t0) / 1000u);
+}
+
+}  // namespace
+
+cudaError_t launch_wait_probe(const uint32_t* word, uint32_t value, uint64_t limit_ns,
+                              uint32_t* out, cudaStream_t st) {
+  k_wait_probe<<<1, 1, 0, st>>>(word, value, limit_ns, out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_upload_keys(const WorldDev* worlds, int nworlds,
                                uint32_t ncells, uint32_t target,

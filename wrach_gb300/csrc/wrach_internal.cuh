@@ -48,7 +48,7 @@ struct Ctrl {
   uint32_t bar_gen;     // grid barrier generation
   uint32_t overflow;    // particles dropped for lack of destination room
   uint32_t frames;      // rebin launches that were frames (not uploads)
-  uint32_t unused0;
+  uint32_t never_set;   // stays 0: the word wrach_selftest_wait waits on
   uint32_t big_count;   // counting sort: cells on the large-cell work list
   uint32_t huge_cells;  // counting sort: cells sorted in global memory, since create
   uint32_t pad[6];
@@ -241,6 +241,19 @@ __device__ __forceinline__ uint64_t global_ns() {
 // Bounded device waits give up after this many nanoseconds and raise
 // kFlagTimeout instead of hanging the GPU.
 constexpr uint64_t kWaitLimitNs = 1000000000ull;
+
+// The device's only kind of wait: until *p differs from `value`, for at most
+// limit_ns of %globaltimer.  Returns false if it gave up (the caller raises
+// kFlagTimeout and carries on, so a lost peer never hangs the GPU).
+__device__ __forceinline__ bool wait_while_equal(const uint32_t* p, uint32_t value,
+                                                 uint64_t limit_ns) {
+  const uint64_t t0 = global_ns();
+  while (ld_acquire_u32(p) == value) {
+    if (global_ns() - t0 > limit_ns) return false;
+    __nanosleep(64);
+  }
+  return true;
+}
 
 // Warp-reduce helpers.
 __device__ __forceinline__ uint32_t warp_max_u32(uint32_t v) {

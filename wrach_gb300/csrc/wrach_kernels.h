@@ -110,6 +110,12 @@ cudaError_t launch_upload_keys(const WorldDev* worlds, int nworlds,
                                uint32_t n_new, const float2* new_pos,
                                uint32_t* keys, cudaStream_t st);
 
+// One thread waits (bounded) while *word == value: out[0] = 1 if the wait
+// gave up, out[1] = microseconds waited.  The wait every device-side wait
+// of the library uses (wait_while_equal).
+cudaError_t launch_wait_probe(const uint32_t* word, uint32_t value, uint64_t limit_ns,
+                              uint32_t* out, cudaStream_t st);
+
 // Reference-layout table of one world (cells + 2 entries) from the global
 // cell-start table.
 cudaError_t launch_world_table(const uint32_t* cell_start, uint32_t cell_off,
