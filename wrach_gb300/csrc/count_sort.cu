@@ -282,7 +282,8 @@ __global__ void __launch_bounds__(kBigThreads) k_cs_big(RebinArgs a) {
     for (uint32_t len = 2; len <= P; len <<= 1) {
       for (uint32_t j = len >> 1; j > 0; j >>= 1) {
         for (uint32_t pi = threadIdx.x; pi < P / 2; pi += kBigThreads) {
-          const uint32_t r = 2 * j * (pi / j) + pi % j, o = r + j;
+          // j is a power of two: r = 2 j floor(pi / j) + pi mod j
+          const uint32_t r = ((pi & ~(j - 1u)) << 1) | (pi & (j - 1u)), o = r + j;
           const uint32_t x = sv[r], y = sv[o];
           if ((x > y) == ((r & len) == 0)) {
             sv[r] = y;
