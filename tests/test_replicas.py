@@ -51,7 +51,7 @@ def _rank_main(rank, port, out):
 
 def test_aggregate_over_two_gloo_ranks():
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.start_processes(_rank_main, args=(port, out), nprocs=2, start_method="spawn")
         assert out[0] == out[1] == (2.0, 300.0)
