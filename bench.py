@@ -50,16 +50,26 @@ def parse():
     p.add_argument("--profile-frames", type=int, default=10)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
-    p.add_argument("--workload", default="lattice", choices=["lattice", "blobs", "surrogate", "batch", "viewport"],
+    p.add_argument("--workload", default="lattice",
+                   choices=["lattice", "blobs", "reference", "surrogate", "batch", "viewport"],
                    help="lattice: the headline line; surrogate and batch print their own line")
     return p.parse_args()
 
 
 def workload(name="lattice"):
-    """The 1M jittered lattice (the headline), or the 4M clustered field
-    (32 Gaussian blobs falling into a basin)."""
+    """The 1M jittered lattice (the headline), the same lattice under the
+    reference's own physics (per-cell Gauss-Seidel, no gravity), or the 4M
+    clustered field (32 Gaussian blobs falling into a basin)."""
     from wrach_gb300 import workloads
     cfg = dict(cell_size=1, mode=1, iterations=4, gravity=0.1)
+    if name == "reference":
+        dims, pos, vel = workloads.lattice()
+        cfg = dict(cell_size=1, mode=0, iterations=1, gravity=0.0)
+        desc = {"workload": "lattice-1M, reference physics", "particles": int(len(pos)),
+                "box": list(dims), "cell_size": 1,
+                "physics": "reference (per-cell Gauss-Seidel, cap 9, no gravity)",
+                "init": "jittered lattice 1334x750 sites, jitter U(-0.25,0.25), vel N(0,1), seed 0"}
+        return dims, pos, vel, cfg, desc
     if name == "blobs":
         dims, pos, vel = workloads.blobs()
         desc = {"workload": "blobs-4M", "particles": int(len(pos)), "box": list(dims),
@@ -231,7 +241,8 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import wrach_gb300 as W
     W.build()
-    dims, pos, vel, cfg, desc = workload("blobs" if args.workload == "blobs" else "lattice")
+    dims, pos, vel, cfg, desc = workload(args.workload if args.workload in ("blobs", "reference")
+                                         else "lattice")
     n = len(pos)
     sim = W.Simulation(W.WrachConfig(dimensions=dims, device=local, **cfg))
     sim.add_particles(pos, vel)
@@ -341,9 +352,11 @@ def run_ours(args):
                "steps": args.e2e_steps,
                "ms_per_step": 1000.0 * max_dt / args.e2e_steps}
 
-    lattice = args.workload != "blobs"
+    lattice = args.workload == "lattice"
+    other = {"blobs": "particle-steps/s at 4M particles, clustered (plain CUDA step)",
+             "reference": "particle-steps/s at 1M particles, the reference's own physics"}
     line = {
-        "metric": METRIC if lattice else "particle-steps/s at 4M particles, clustered (plain CUDA step)",
+        "metric": METRIC if lattice else other[args.workload],
         "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
         "higher_is_better": True, "scaling": "weak",
