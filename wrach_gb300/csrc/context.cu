@@ -539,7 +539,14 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) return oom(e);
   const size_t tc = ctx->total_cap;
-  if ((e = dalloc(&ctx->worlds_d, nworlds)) != cudaSuccess) return oom(e);
+  // the worlds, then (batches) the first world of each tile of cells
+  const size_t tiles_words = nworlds > 1 ? (size_t)wrach::world_tiles(ctx->ncells) + 2 : 0;
+  const size_t worlds_words = (nworlds * sizeof(WorldDev) + 3) / 4 + tiles_words;
+  {
+    uint32_t* raw = nullptr;
+    if ((e = dalloc(&raw, worlds_words)) != cudaSuccess) return oom(e);
+    ctx->worlds_d = reinterpret_cast<WorldDev*>(raw);
+  }
   if ((e = dalloc(&ctx->pos, tc)) != cudaSuccess) return oom(e);
   if ((e = dalloc(&ctx->vel, tc)) != cudaSuccess) return oom(e);
   if ((e = dalloc(&ctx->pos_o, tc)) != cudaSuccess) return oom(e);
@@ -579,6 +586,20 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   if ((e = cudaMemcpy(ctx->worlds_d, ctx->worlds_h.data(), nworlds * sizeof(WorldDev),
                       cudaMemcpyHostToDevice)) != cudaSuccess)
     return oom(e);
+  if (tiles_words) {
+    static_assert(sizeof(WorldDev) % 4 == 0, "the tile table follows the worlds word-aligned");
+    std::vector<uint32_t> first(tiles_words);
+    uint32_t wi = 0;
+    for (size_t t = 0; t < tiles_words; ++t) {
+      const uint64_t c = std::min<uint64_t>((uint64_t)t << wrach::kWorldTileShift, ctx->ncells - 1);
+      while (wi + 1 < nworlds && ctx->worlds_h[wi + 1].cell_off <= c) ++wi;
+      first[t] = wi;
+    }
+    first[tiles_words - 2] = first[tiles_words - 1] = nworlds - 1;
+    if ((e = cudaMemcpy(reinterpret_cast<uint32_t*>(ctx->worlds_d + nworlds), first.data(),
+                        tiles_words * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return oom(e);
+  }
   if (ensure_sort_capacity(ctx, tc) != WRACH_OK) {
     int rc = WRACH_ERR_OUT_OF_MEMORY;
     release(ctx);

@@ -74,9 +74,21 @@ __device__ __forceinline__ void cell_xy(const WorldDev& w, uint32_t local,
 }
 
 // World of a global cell index: the last world whose cell_off <= c.
+// With more than one world, the array of nworlds WorldDev is followed by
+// world_tiles(ncells) + 2 u32: the world holding the first cell of each tile
+// of 2^kWorldTileShift cells (the last two entries: nworlds - 1), so a
+// lookup searches only the few worlds one tile can span.
+constexpr uint32_t kWorldTileShift = 12;
+__host__ __device__ __forceinline__ uint32_t world_tiles(uint32_t ncells) {
+  return (ncells + (1u << kWorldTileShift) - 1) >> kWorldTileShift;
+}
+
 __device__ __forceinline__ int world_of_cell(const WorldDev* __restrict__ W,
                                              int nworlds, uint32_t c) {
-  int lo = 0, hi = nworlds - 1;
+  if (nworlds <= 1) return 0;
+  const uint32_t* tile_first = reinterpret_cast<const uint32_t*>(W + nworlds);
+  const uint32_t t = c >> kWorldTileShift;
+  int lo = (int)__ldg(tile_first + t), hi = (int)__ldg(tile_first + t + 1);
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
     if (__ldg(&W[mid].cell_off) <= c)
