@@ -51,7 +51,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--workload", default="lattice",
-                   choices=["lattice", "blobs", "reference", "surrogate", "batch", "viewport"],
+                   choices=["lattice", "blobs", "small", "reference", "surrogate", "batch", "viewport"],
                    help="lattice: the headline line; surrogate and batch print their own line")
     return p.parse_args()
 
@@ -62,6 +62,13 @@ def workload(name="lattice"):
     clustered field (32 Gaussian blobs falling into a basin)."""
     from wrach_gb300 import workloads
     cfg = dict(cell_size=1, mode=1, iterations=4, gravity=0.1)
+    if name == "small":
+        dims, pos, vel = workloads.small()
+        desc = {"workload": "small-16K", "particles": int(len(pos)), "box": list(dims),
+                "cell_size": 1, "physics": "extended (3x3 cells, 4 Jacobi iterations)",
+                "gravity": 0.1, "init": "uniform in 512x512, vel N(0,2), seed 0",
+                "note": "2.6 MB of state: L2-resident and launch-bound, not rooflined"}
+        return dims, pos, vel, cfg, desc
     if name == "reference":
         dims, pos, vel = workloads.lattice()
         cfg = dict(cell_size=1, mode=0, iterations=1, gravity=0.0)
@@ -241,7 +248,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import wrach_gb300 as W
     W.build()
-    dims, pos, vel, cfg, desc = workload(args.workload if args.workload in ("blobs", "reference")
+    dims, pos, vel, cfg, desc = workload(args.workload if args.workload in ("blobs", "reference", "small")
                                          else "lattice")
     n = len(pos)
     sim = W.Simulation(W.WrachConfig(dimensions=dims, device=local, **cfg))
@@ -354,7 +361,8 @@ def run_ours(args):
 
     lattice = args.workload == "lattice"
     other = {"blobs": "particle-steps/s at 4M particles, clustered (plain CUDA step)",
-             "reference": "particle-steps/s at 1M particles, the reference's own physics"}
+             "reference": "particle-steps/s at 1M particles, the reference's own physics",
+             "small": "particle-steps/s at 16K particles (plain CUDA step)"}
     line = {
         "metric": METRIC if lattice else other[args.workload],
         "value": value, "unit": "particle-steps/s", "n_gpus": world,
@@ -423,6 +431,31 @@ def run_surrogate(args):
     loss = sim.surrogate_train(4000, 16384, 2e-3)
     train_s = time.perf_counter() - t0
     net, zero = sim.surrogate_evaluate()
+    # the network alone on the tensor cores: features of the current frame
+    # precomputed, then the forward kernel timed with CUDA events
+    x = torch.zeros((n, 64), dtype=torch.int16, device="cuda")
+    yout = torch.zeros((n, 2), dtype=torch.float32, device="cuda")
+    sim.surrogate_features(x.data_ptr(), n)
+    sim.sync()
+    fstream = torch.cuda.ExternalStream(sim.stream)
+    for _ in range(3):
+        sim.surrogate_forward(x.data_ptr(), n, yout.data_ptr())
+    sim.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    e0.record(fstream)
+    for _ in range(reps):
+        sim.surrogate_forward(x.data_ptr(), n, yout.data_ptr())
+    e1.record(fstream)
+    torch.cuda.synchronize()
+    fwd_s = e0.elapsed_time(e1) / 1000.0 / reps
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16_peak, peak_source = float(json.load(f)["bf16_tflops"]), "measured (burst)"
+    except Exception:
+        bf16_peak, peak_source = 1900.0, "fallback"
+    flop_per_particle = 2 * (50 * 64 + 64 * 64 + 64 * 2)  # the unpadded network
+    net_tflops = flop_per_particle * n / fwd_s / 1e12
     frames = 1000 if args.steps >= 1000 else max(64, args.steps)
     stream = torch.cuda.ExternalStream(sim.stream)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -455,6 +488,11 @@ def run_surrogate(args):
                           "reference_penetration_px": st["reference_penetration"],
                           "max_energy_drift": st["max_energy_drift"]},
             "speedup_vs_plain": plain_s / sur_s,
+            "network_roofline": {"bound": "tensor", "kernel": "k_mlp_forward (features precomputed)",
+                                 "achieved": net_tflops, "peak": bf16_peak, "peak_source": peak_source,
+                                 "unit": "TFLOP/s", "frac": net_tflops / bf16_peak,
+                                 "flop_per_particle": flop_per_particle, "ms": 1000 * fwd_s,
+                                 "note": "mma.sync m16n8k16 BF16, FP32 accumulate; the GELUs (erf) are most of its instructions"},
             "final_frame": {"plain_mean_penetration_px": pen_plain[0],
                             "surrogate_mean_penetration_px": pen_sur[0],
                             "excess_penetration_px": pen_sur[0] - pen_plain[0],

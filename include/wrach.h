@@ -186,6 +186,13 @@ uint32_t wrach_num_worlds(WrachContext *ctx);
 
 int wrach_sync(WrachContext *ctx);
 
+/* The cell key of each of the world's frame particles, in frame order:
+ * cy * gx + cx, the key the reference's count pass computes
+ * (particles_per_cell.wgsl:14-27), world-local.  `keys` takes at least the
+ * frame's particle count (particles_in_frame_count) entries.  Blocks. */
+int wrach_read_keys(WrachContext *ctx, uint32_t world, uint32_t *keys,
+                    uint32_t capacity);
+
 /* Sticky device flags (WRACH_FLAG_*) seen since create; blocks. */
 int wrach_flags(WrachContext *ctx, uint32_t *flags);
 

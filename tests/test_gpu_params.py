@@ -68,3 +68,31 @@ def test_other_physics_constants(W, O, mode):
     cfg = W.WrachConfig(dimensions=dims, cell_size=2, mode=mode, iterations=3, gravity=0.3,
                         min_distance=1.5, max_velocity=2.0, capacity=6000)
     _run(W, O, cfg, pos, vel, [1, 6, 15])
+
+
+def test_read_keys_match_the_table(W, O):
+    # single world and one world of a batch: each frame particle's key is the
+    # cell the table places it in, cy * gx + cx
+    pos, vel = _field(24, 2500, (0.0, 0.0), (40.0, 30.0))
+    cfg = W.WrachConfig(dimensions=(40.0, 30.0), cell_size=1, mode=1, iterations=4, gravity=0.1,
+                        capacity=5000)
+    with W.Simulation(cfg) as sim:
+        sim.add_particles(pos, vel)
+        sim.step(3)
+        p, v, table = sim.read_frame()
+        keys = sim.read_keys()
+        want = np.repeat(np.arange(len(table) - 2), np.diff(table[1:].astype(np.int64)))
+        assert np.array_equal(keys, want.astype(np.uint32))
+        w = O.world(40.0, 30.0, 1)
+        oracle_keys = np.array([O.frame_key(w, float(x), float(y))[0] for x, y in p], np.uint32)
+        assert np.array_equal(keys, oracle_keys)
+    dims = [(30.0, 20.0), (25.0, 35.0)]
+    with W.Simulation(W.WrachConfig(cell_size=1, mode=0, capacity=3000), worlds=dims) as sim:
+        for k, d in enumerate(dims):
+            q, u = _field(30 + k, 800, (0.0, 0.0), d)
+            sim.set_particles(q, u, world=k)
+        sim.step(2)
+        p, v, table = sim.read_frame(world=1)
+        keys = sim.read_keys(world=1)
+        want = np.repeat(np.arange(len(table) - 2), np.diff(table[1:].astype(np.int64)))
+        assert np.array_equal(keys, want.astype(np.uint32))

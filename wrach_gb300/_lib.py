@@ -127,6 +127,7 @@ SIGNATURES = {
     "wrach_frame_metrics": (ctypes.c_int, [_P, _F, _F, _F]),
     "wrach_surrogate_correction": (ctypes.c_int, [_P, _P]),
     "wrach_write_back": (ctypes.c_int, [_P, ctypes.c_uint32]),
+    "wrach_read_keys": (ctypes.c_int, [_P, ctypes.c_uint32, _U, ctypes.c_uint32]),
     "wrach_selftest_wait": (ctypes.c_int, [_P, ctypes.c_uint32, _U, _U]),
     "wrach_set_viewport": (ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_float, ctypes.c_float]),
     "wrach_store_size": (ctypes.c_int, [_P, ctypes.c_uint32, _U]),

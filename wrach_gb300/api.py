@@ -190,6 +190,13 @@ class Simulation:
         n = int(idx[-1])
         return pos[:n], vel[:n], idx
 
+    def read_keys(self, world=0):
+        """The cell key (cy * gx + cx) of each frame particle, in frame order."""
+        n = int(self.settings(world).particles_in_frame_count)
+        keys = np.zeros(max(n, 1), np.uint32)
+        self._check(self._L.wrach_read_keys(self._ctx, world, _u32p(keys), max(n, 1)))
+        return keys[:n]
+
     def render(self, width_px, height_px, world=0):
         """The frame drawn as the reference's draw pass does: an 8-bit image
         (height_px, width_px), row 0 at the top."""

@@ -1292,6 +1292,25 @@ int wrach_get_settings(WrachContext* ctx, uint32_t world, WrachWorldSettings* ou
   return WRACH_OK;
 }
 
+int wrach_read_keys(WrachContext* ctx, uint32_t world, uint32_t* keys, uint32_t capacity) {
+  if (!ctx) return WRACH_ERR_INVALID_ARGUMENT;
+  if (world >= ctx->nworlds) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "world out of range");
+  const uint32_t n = ctx->n_h[world], off = ctx->poff_h[world];
+  if (n && (!keys || capacity < n)) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "key buffer too small");
+  DeviceGuard guard(ctx->device);
+  if (n) {
+    // the keys land in the scratch the sort uses between frames
+    int rc = ensure_sort_capacity(ctx, (size_t)n);
+    if (rc) return rc;
+    CK(wrach::launch_local_keys(ctx->cell_of[ctx->cur] + off, n, ctx->worlds_h[world].cell_off,
+                                ctx->iB, ctx->stream));
+    ctx->launches += 1;
+    CK(cudaMemcpyAsync(keys, ctx->iB, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return WRACH_OK;
+}
+
 int wrach_write_back(WrachContext* ctx, uint32_t world) {
   if (!ctx) return WRACH_ERR_INVALID_ARGUMENT;
   if (world >= ctx->nworlds) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "world out of range");

@@ -473,6 +473,23 @@ cudaError_t launch_upload_keys(const WorldDev* worlds, int nworlds,
   return cudaGetLastError();
 }
 
+namespace {
+
+__global__ void k_local_keys(const uint32_t* __restrict__ cell_of, uint32_t n, uint32_t cell_off,
+                             uint32_t* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = cell_of[i] - cell_off;
+}
+
+}  // namespace
+
+cudaError_t launch_local_keys(const uint32_t* cell_of, uint32_t n, uint32_t cell_off,
+                              uint32_t* out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_local_keys<<<(n + 255) / 256, 256, 0, st>>>(cell_of, n, cell_off, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_world_table(const uint32_t* cell_start, uint32_t cell_off,
                                uint32_t cells, uint32_t* out, cudaStream_t st) {
   const uint32_t n = cells + 1;

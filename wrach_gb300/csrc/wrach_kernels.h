@@ -116,6 +116,10 @@ cudaError_t launch_upload_keys(const WorldDev* worlds, int nworlds,
 cudaError_t launch_wait_probe(const uint32_t* word, uint32_t value, uint64_t limit_ns,
                               uint32_t* out, cudaStream_t st);
 
+// World-local cell keys (cell_of - cell_off) of n frame particles.
+cudaError_t launch_local_keys(const uint32_t* cell_of, uint32_t n, uint32_t cell_off,
+                              uint32_t* out, cudaStream_t st);
+
 // Reference-layout table of one world (cells + 2 entries) from the global
 // cell-start table.
 cudaError_t launch_world_table(const uint32_t* cell_start, uint32_t cell_off,
