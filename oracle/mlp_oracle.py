@@ -9,7 +9,7 @@ wrach_gb300/csrc/surrogate.cu:
              the 5x5 cells around its cell by binary32 squared distance,
              ties by index, each as (dx, dy, dvx, dvy) relative to the
              particle; then its velocity; zero padding to 64; rounded to BF16.
-  network    64 -> 64 -> 64 -> 2, GELU (erf) after the hidden layers, BF16
+  network    64 -> 64 -> 64 -> 2, GELU (tanh form) after the hidden layers, BF16
              weights and activations, accumulation in float64 here (FP32 on
              the GPU).
   gradients  of L = 0.5 * mean over rows of |y - t|^2, with the BF16
@@ -54,17 +54,18 @@ def pack(w1, b1, w2, b2, w3, b3):
     return np.concatenate([w1.ravel(), b1, w2.ravel(), b2, w3.ravel(), b3]).astype(np.float32)
 
 
-_erf = np.vectorize(math.erf)
+# GELU in its tanh form (Hendrycks & Gimpel, 2016), as the CUDA kernels
+# compute it (there with the hardware tanh, relative error about 2^-11)
+_C, _A = math.sqrt(2.0 / math.pi), 0.044715
 
 
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    return 0.5 * z * (1.0 + np.tanh(_C * (z + _A * z ** 3)))
 
 
 def gelu_grad(z):
-    cdf = 0.5 * (1.0 + _erf(z / math.sqrt(2.0)))
-    pdf = np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
-    return cdf + z * pdf
+    t = np.tanh(_C * (z + _A * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _C * (1.0 + 3.0 * _A * z * z)
 
 
 def _q(a, on):

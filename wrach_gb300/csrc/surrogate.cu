@@ -6,7 +6,7 @@
 //             5x5 cells around the particle (squared distance, ties by index),
 //             each as (dx, dy, dvx, dvy) relative to the particle, then the
 //             particle's own velocity; 50 values padded to 64, BF16.
-//   network   64 -> 64 -> 64 -> 2 (padded to 8), GELU (erf form) after the
+//   network   64 -> 64 -> 64 -> 2 (padded to 8), GELU (tanh form) after the
 //             two hidden layers; BF16 weights, FP32 accumulation, on the
 //             tensor cores with mma.sync m16n8k16 (one warp per 16 rows; the
 //             accumulator fragment of one layer is the A fragment of the
@@ -41,13 +41,26 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ float gelu(float x) {
-  return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+// GELU in its tanh form, 0.5 x (1 + tanh(c (x + a x^3))), c = sqrt(2/pi),
+// a = 0.044715 (Hendrycks & Gimpel, 2016), with the hardware tanh
+// (tanh.approx.f32, relative error about 2^-11, below the BF16 rounding the
+// activations then get).
+constexpr float kGeluC = 0.7978845608028654f, kGeluA = 0.044715f;
+
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
 }
+__device__ __forceinline__ float gelu(float x) {
+  const float t = tanh_hw(kGeluC * x * (1.0f + kGeluA * x * x));
+  return 0.5f * x * (1.0f + t);
+}
+// d/dx: 0.5 (1 + t) + 0.5 x (1 - t^2) c (1 + 3 a x^2)
 __device__ __forceinline__ float gelu_grad(float x) {
-  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
-  return cdf + x * pdf;
+  const float x2 = x * x;
+  const float t = tanh_hw(kGeluC * x * (1.0f + kGeluA * x2));
+  return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * kGeluC * (1.0f + 3.0f * kGeluA * x2);
 }
 
 // Shared-memory copy of the network for the forward pass: the weights as
@@ -583,35 +596,50 @@ __device__ __forceinline__ bool knn_row(const WorldDev* __restrict__ worlds, int
   const int y0 = max((int)cy - 2, 0), y1 = min((int)cy + 2, (int)w.gy - 1);
   const uint32_t x0 = cx >= 2 ? cx - 2 : 0, x1 = min(cx + 2, w.gx - 1);
   const uint32_t ncol = x1 - x0 + 1;  // 3 to 5 cells per row
+  // one candidate: insert (distance, index), keeping the list ascending;
+  // every comparison against the old list first, then the shift
+  auto consider = [&](uint32_t j) {
+    const float2 pj = pos[j];
+    const float dx = __fsub_rn(pj.x, pi.x), dy = __fsub_rn(pj.y, pi.y);
+    const float d = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+    if (!(d < bd[kK - 1]) && !(d == bd[kK - 1] && j < bj[kK - 1])) return;
+    bool lt[kK];
+#pragma unroll
+    for (uint32_t k = 0; k < kK; ++k) lt[k] = d < bd[k] || (d == bd[k] && j < bj[k]);
+#pragma unroll
+    for (uint32_t k = kK - 1; k > 0; --k) {
+      bd[k] = lt[k - 1] ? bd[k - 1] : (lt[k] ? d : bd[k]);
+      bj[k] = lt[k - 1] ? bj[k - 1] : (lt[k] ? j : bj[k]);
+    }
+    bd[0] = lt[0] ? d : bd[0];
+    bj[0] = lt[0] ? j : bj[0];
+  };
   for (int ny = y0; ny <= y1; ++ny) {
     // the row's table entries first: independent loads
     const uint32_t rb = w.cell_off + (uint32_t)ny * w.gx + x0;
     uint32_t st[6];
 #pragma unroll
     for (uint32_t k = 0; k < 6; ++k) st[k] = k <= ncol ? cell_start[rb + k] : 0u;
+    // a row whose cells before the last are within capacity is one
+    // contiguous range of candidates (the last cell clipped to capacity)
+    bool merged = true;
+#pragma unroll
+    for (uint32_t col = 0; col + 1 < 5; ++col)
+      if (col + 1 < ncol && st[col + 1] - st[col] > ph.cap) merged = false;
+    if (merged) {
+      const uint32_t last = ncol == 5 ? st[4] : (ncol == 4 ? st[3] : st[2]);
+      const uint32_t end = ncol == 5 ? st[5] : (ncol == 4 ? st[4] : st[3]);
+      const uint32_t e = min(end, last + ph.cap);
+      for (uint32_t j = st[0]; j < e; ++j)
+        if (j != i) consider(j);
+      continue;
+    }
 #pragma unroll
     for (uint32_t col = 0; col < 5; ++col) {
       if (col >= ncol) break;
       const uint32_t js = st[col], je = min(st[col + 1], js + ph.cap);
-      for (uint32_t j = js; j < je; ++j) {
-        if (j == i) continue;
-        const float2 pj = pos[j];
-        const float dx = __fsub_rn(pj.x, pi.x), dy = __fsub_rn(pj.y, pi.y);
-        float d = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-        if (!(d < bd[kK - 1]) && !(d == bd[kK - 1] && j < bj[kK - 1])) continue;
-        // insert, keeping (distance, index) ascending: every comparison
-        // against the old list first, then the shift (no serial chain)
-        bool lt[kK];
-#pragma unroll
-        for (uint32_t k = 0; k < kK; ++k) lt[k] = d < bd[k] || (d == bd[k] && j < bj[k]);
-#pragma unroll
-        for (uint32_t k = kK - 1; k > 0; --k) {
-          bd[k] = lt[k - 1] ? bd[k - 1] : (lt[k] ? d : bd[k]);
-          bj[k] = lt[k - 1] ? bj[k - 1] : (lt[k] ? j : bj[k]);
-        }
-        bd[0] = lt[0] ? d : bd[0];
-        bj[0] = lt[0] ? j : bj[0];
-      }
+      for (uint32_t j = js; j < je; ++j)
+        if (j != i) consider(j);
     }
   }
 #pragma unroll
