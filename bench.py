@@ -492,7 +492,7 @@ def run_surrogate(args):
                                  "achieved": net_tflops, "peak": bf16_peak, "peak_source": peak_source,
                                  "unit": "TFLOP/s", "frac": net_tflops / bf16_peak,
                                  "flop_per_particle": flop_per_particle, "ms": 1000 * fwd_s,
-                                 "note": "mma.sync m16n8k16 BF16, FP32 accumulate; the GELUs (erf) are most of its instructions"},
+                                 "note": "mma.sync m16n8k16 BF16, FP32 accumulate; tanh-form GELU on tanh.approx.f32"},
             "final_frame": {"plain_mean_penetration_px": pen_plain[0],
                             "surrogate_mean_penetration_px": pen_sur[0],
                             "excess_penetration_px": pen_sur[0] - pen_plain[0],
