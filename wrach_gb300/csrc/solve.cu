@@ -93,11 +93,12 @@ k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
 // cells in row-major order, table order inside a cell), so the sum is
 // deterministic.
 //
-// Per neighbour row, two passes: pass 1 marks the candidates within reach
-// with an exact squared-distance test (cheap, every lane), pass 2 applies
+// Two passes: pass 1 marks, per neighbour row, the candidates within reach
+// with an exact squared-distance test (cheap, every lane); pass 2 applies
 // the reference's push (IEEE square root and division) to those only, in
-// candidate order.  A row whose cells are all within capacity is one
-// contiguous range of candidates and is scanned in one loop.
+// candidate order, in one loop over the three rows' marks.  A row whose
+// cells before the last are within capacity is one contiguous range of
+// candidates, scanned in one loop; other rows keep 16 mark bits per cell.
 //
 // FINAL fuses gravity, integration, boundaries, the velocity clamp and the
 // key emission.  METRICS (final pass only) also writes the block's sums for
@@ -108,14 +109,6 @@ k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
 // [4] the kinetic energy a plain frame gives (gravity, the clamp and wall
 // reflections only change the velocity).  A launch whose `run_if` flag reads
 // 0 returns at once.
-// Candidate index of mask bit b of a neighbour row: contiguous rows map bit
-// b to s0 + b; rows with an over-full cell keep 16 bits per cell.
-__device__ __forceinline__ uint32_t row_candidate(bool merged, uint32_t s0, uint32_t s1,
-                                                  uint32_t s2, uint32_t b) {
-  if (merged) return s0 + b;
-  return (b < 16 ? s0 : (b < 32 ? s1 - 16 : s2 - 32)) + b;
-}
-
 template <bool FINAL, bool METRICS>
 __global__ void __launch_bounds__(512)
 k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
@@ -163,6 +156,10 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
       }
       const uint32_t ncol = x1 - x0 + 1;  // 2 or 3 cells per row
       static_assert(kMaxCellCapacity <= 16, "16 mask bits per cell");
+      // per row: the close mask and the map from mask bit b to candidate
+      // index, base + b + (b >= 16 ? adj1 : 0) + (b >= 32 ? adj2 : 0)
+      uint64_t rmask[3];
+      uint32_t rbase[3], radj1[3], radj2[3];
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
         // the row's taking-part candidates: up to three cells of at most
@@ -174,50 +171,68 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
         const uint32_t e2 = ncol == 3 ? min(s3, s2 + ph.cap) : s2;
         uint64_t close = 0;
         const bool merged = e0 == s1 && (ncol == 2 || e1 == s2);
+        rbase[r] = s0;
+        radj1[r] = merged ? 0u : s1 - s0 - 16u;
+        radj2[r] = merged ? 0u : s2 - s1 - 16u;
         if (merged) {
           // no over-full cell before the last: one contiguous range, two
-          // candidates per step
+          // candidates per step (an odd last step tests its one candidate
+          // twice and keeps the first result)
           const uint32_t e = ncol == 3 ? e2 : e1;
-          uint32_t j = s0;
-          for (; j + 1 < e; j += 2) {
-            const f32x2 da = f2_sub(q64[j], qi2), db = f2_sub(q64[j + 1], qi2);
+          for (uint32_t j = s0; j < e; j += 2) {
+            const uint32_t j1 = min(j + 1, e - 1);
+            const f32x2 da = f2_sub(q64[j], qi2), db = f2_sub(q64[j1], qi2);
             const bool ca = !(f2_len2(da) >= ph.skip_d2);
-            const bool cb = !(f2_len2(db) >= ph.skip_d2);
+            const bool cb = j + 1 < e && !(f2_len2(db) >= ph.skip_d2);
             close |= (uint64_t)((ca ? 1u : 0u) | (cb ? 2u : 0u)) << (j - s0);
           }
-          if (j < e) {
-            if (!(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << (j - s0);
-          }
-          // the particle itself is not its own neighbour
-          if (i >= s0 && i < e) close &= ~(1ull << (i - s0));
+          // the particle itself (in the middle row) is not its own neighbour
+          if (r == 1 && i >= s0 && i < e) close &= ~(1ull << (i - s0));
         } else {
           uint32_t k = 0;
           for (uint32_t j = s0; j < e0; ++j, ++k) {
-            if (j != i && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
+            if ((r != 1 || j != i) && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
           }
           k = 16;
           for (uint32_t j = s1; j < e1; ++j, ++k) {
-            if (j != i && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
+            if ((r != 1 || j != i) && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
           }
           k = 32;
           for (uint32_t j = s2; j < e2; ++j, ++k) {
-            if (j != i && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
+            if ((r != 1 || j != i) && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
           }
         }
-        // pass 2: the reference's push for those, in candidate order
-        // (cell.rs:79-95)
-        while (close) {
-          const uint32_t b = __ffsll((long long)close) - 1;
-          close &= close - 1;
-          const uint32_t j = row_candidate(merged, s0, s1, s2, b);
-          const f32x2 dd = f2_sub(q64[j], qi2);
-          float f, d;
-          if (!push_factor(f2_x(dd), f2_y(dd), ph.min_d, ph.skip_d2, f, d)) continue;
-          if (METRICS) pen = fmaxf(pen, __fsub_rn(ph.min_d, d));
-          // scalar: a paired multiply feeding a paired add may be fused
-          ax = __fadd_rn(ax, __fmul_rn(f2_x(dd), f));
-          ay = __fadd_rn(ay, __fmul_rn(f2_y(dd), f));
+        rmask[r] = close;
+      }
+      // pass 2: the reference's push for those, in candidate order
+      // (cell.rs:79-95).  One loop over the three rows' masks, so that a
+      // lane moves on to its next row without waiting for the warp's other
+      // lanes to finish the current one.
+      uint64_t cur = rmask[0];
+      uint32_t base = rbase[0], adj1 = radj1[0], adj2 = radj2[0];
+      uint64_t next1 = rmask[1], next2 = rmask[2];
+      for (;;) {
+        if (cur == 0) {
+          if (next1) {
+            cur = next1; next1 = 0;
+            base = rbase[1]; adj1 = radj1[1]; adj2 = radj2[1];
+          } else if (next2) {
+            cur = next2; next2 = 0;
+            base = rbase[2]; adj1 = radj1[2]; adj2 = radj2[2];
+          } else {
+            break;
+          }
         }
+        const uint32_t b = __ffsll((long long)cur) - 1;
+        cur &= cur - 1;
+        const uint32_t j = base + b + (b >= 16 ? adj1 : 0u) + (b >= 32 ? adj2 : 0u);
+        const f32x2 dd = f2_sub(q64[j], qi2);
+        float d;
+        const float f = push_factor_within(f2_x(dd), f2_y(dd), ph.min_d, d);
+        if (METRICS) pen = fmaxf(pen, __fsub_rn(ph.min_d, d));
+        // scalar: a paired multiply feeding a paired add may be fused
+        ax = __fadd_rn(ax, __fmul_rn(f2_x(dd), f));
+        ay = __fadd_rn(ay, __fmul_rn(f2_y(dd), f));
       }
     }
   }

@@ -154,6 +154,16 @@ __device__ __forceinline__ bool push_factor(float ex, float ey, float min_d,
   float d;
   return push_factor(ex, ey, min_d, skip_d2, f, d);
 }
+// The same force for a pair already found within reach (s < skip_d2, or s
+// NaN): both tests of push_factor would pass, so they are left out.
+__device__ __forceinline__ float push_factor_within(float ex, float ey, float min_d,
+                                                    float& dist) {
+  const float s = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+  float d = __fsqrt_rn(s);
+  dist = d;
+  if (d == 0.0f) d = 0.0001f;
+  return __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(min_d, d)), d);
+}
 
 // Counting-sort ticket of a particle whose next cell is k (k >= ncells: no
 // cell).  All 32 lanes of the warp call it together.  Per warp, one atomic
