@@ -539,10 +539,16 @@ def run_batch(args):
     torch.cuda.synchronize()
     steps = max(10, min(args.steps, 500))
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local).start()
+    time.sleep(0.25)
+    torch.cuda.synchronize()
+    l0 = sim.kernel_launches
     start.record(stream)
     sim.step(steps)
     end.record(stream)
     torch.cuda.synchronize()
+    launches = sim.kernel_launches - l0
+    clocks.stop()
     ms = start.elapsed_time(end)
     st = sim.stats()
     max_s, units = replicas.aggregate(ms / 1000.0, n * steps, device="cuda")
@@ -553,6 +559,7 @@ def run_batch(args):
             "config": {"workload": "batch-256", "worlds_on_rank_0": len(poss), "particles_on_rank_0": n,
                        "cells": st["cells"], "physics": "extended (4 iterations, gravity 0.1)",
                        "l2": "working set above L2 (tables of %d cells)" % st["cells"]},
+            "gpu_launches": launches, "clocks": clocks.summary(),
             "autotune": {"choice": {"cell_size": tuned.cell_size, "rebin_blocks": tuned.rebin_blocks,
                                     "solve_block": tuned.solve_block},
                          "ms_per_frame": table, "seconds": tune_s}}
