@@ -83,6 +83,9 @@ uint32_t bits_for(uint32_t v) {
 struct WrachContext {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // a frame's large-cell sort runs on `aux`, beside the small cells' pass
+  cudaStream_t aux = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   WrachConfig cfg{};
   PhysDev ph{};
   uint32_t nworlds = 0;
@@ -204,6 +207,9 @@ void release(WrachContext* ctx) {
     dfree(s.pos);
     dfree(s.vel);
   }
+  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+  if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
+  if (ctx->aux) cudaStreamDestroy(ctx->aux);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
 }
 
@@ -362,8 +368,21 @@ int enqueue_frame(WrachContext* ctx) {
   r.vel_dst = ctx->vel;
   r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
   r.force_general = 0;
+  // the large cells' sort (the last step) writes other slots than the small
+  // cells' pass before it, so outside per-launch profiling it runs on the
+  // auxiliary stream at the same time, joined back before the frame ends
+  const bool fork = !ctx->event_hook && r.n;
   for (int step = tickets_taken ? 1 : 0; step < wrach::kCountSortSteps; ++step) {
     bool launched;
+    if (fork && step == wrach::kCountSortSteps - 2) {
+      CK(cudaEventRecord(ctx->fork_ev, st));
+      CK(cudaStreamWaitEvent(ctx->aux, ctx->fork_ev, 0));
+      CK(wrach::launch_count_sort_step(r, step + 1, ctx->sms, ctx->aux, &launched));
+      CK(cudaEventRecord(ctx->join_ev, ctx->aux));
+      CK(wrach::launch_count_sort_step(r, step, ctx->sms, st, &launched));
+      CK(cudaStreamWaitEvent(st, ctx->join_ev, 0));
+      break;
+    }
     CK(wrach::launch_count_sort_step(r, step, ctx->sms, st, &launched));
     if (launched) mark(ctx);
   }
@@ -538,6 +557,9 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   };
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) return oom(e);
+  if ((e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking)) != cudaSuccess) return oom(e);
+  if ((e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming)) != cudaSuccess) return oom(e);
+  if ((e = cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming)) != cudaSuccess) return oom(e);
   const size_t tc = ctx->total_cap;
   // the worlds, then (batches) the first world of each tile of cells
   const size_t tiles_words = nworlds > 1 ? (size_t)wrach::world_tiles(ctx->ncells) + 2 : 0;

@@ -13,18 +13,20 @@
 //   scan     exclusive scan of the per-cell counts, one block per tile of
 //            2048 cells; a tile's prefix is the sum of the earlier tiles'
 //            sums (already final, so no block waits); it writes the
-//            cell-start table and clears the counts
+//            cell-start table, clears the counts and lists the cells of more
+//            than kSmallCell particles (the pass that takes the tickets
+//            empties that list first)
 //   scatter  source index and cell of every particle to table start + ticket
 //            (arrival order inside a cell)
 //   place    the stable order: inside a cell, a particle's rank is the number
 //            of the cell's particles with a smaller source index; then the
 //            gather of positions, velocities and cells into that slot.  Cells
-//            of up to kSmallCell particles are ranked by one thread per slot;
-//            larger ones go to a work list
+//            of up to kSmallCell particles are ranked by one thread per slot
 //   cells    one block per listed cell: up to kBigCell particles a bitonic
 //            sort of the source indices in shared memory, more than that a
 //            block-wide LSD radix sort of them in global memory; then the
-//            gather
+//            gather.  It writes other slots than place, so the two may run
+//            at the same time
 //
 // The result is the stable order (a cell's particles keep their source
 // order), the order of the oracle's counting sort and of rebin.cu's radix
@@ -44,6 +46,7 @@ __global__ void __launch_bounds__(256) k_cs_count(RebinArgs a) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t lane = threadIdx.x & 31;
+  if (i == 0) a.ctrl->big_count = 0u;  // the scan lists this rebin's large cells
   // whole warps walk the particles, so every lane takes part in the match
   for (uint32_t base = i - lane; base < a.n; base += stride) {
     const uint32_t j = base + lane;
@@ -72,10 +75,7 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
   __shared__ uint32_t warp_sum[kScanThreads / 32], red[kScanThreads / 32];
   const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const uint32_t tile = blockIdx.x, n = a.ncells;
-  if (tile == 0 && t == 0) {
-    a.ctrl->big_count = 0u;
-    if (!a.force_general) a.ctrl->frames += 1;
-  }
+  if (tile == 0 && t == 0 && !a.force_general) a.ctrl->frames += 1;
   const uint32_t c0 = tile * kScanTile + t * kScanPer;
   uint32_t v[kScanPer];
   if (c0 + kScanPer <= n) {
@@ -112,6 +112,15 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
     total += warp_sum[w];
   }
   uint32_t run = prefix + before + x - sum;
+  // the large cells' work list (at most n / (kSmallCell + 1) cells qualify,
+  // and big_cap is larger)
+#pragma unroll
+  for (uint32_t u = 0; u < kScanPer; ++u) {
+    if (v[u] > kSmallCell) {
+      const uint32_t w = atomicAdd(&a.ctrl->big_count, 1u);
+      if (w < a.big_cap) a.big_list[w] = c0 + u;
+    }
+  }
   if (c0 + kScanPer <= n) {
     uint4* dst = reinterpret_cast<uint4*>(a.cs_new + c0);
     uint4* cnt = reinterpret_cast<uint4*>(a.counts + c0);
@@ -174,21 +183,15 @@ __global__ void __launch_bounds__(256) k_cs_place(RebinArgs a) {
   uint32_t overflow = 0;
   // the guards below only matter if the scan timed out (table inconsistent)
   const uint32_t k = q < total && q < a.n ? a.cell_tmp[q] : a.ncells;
-  const uint32_t s0 = k < a.ncells ? a.cs_new[k] : 0u;
-  const uint32_t s1 = k < a.ncells ? min(a.cs_new[k + 1], min(total, a.n)) : 0u;
-  if (k < a.ncells && s0 < s1) {
-    if (s1 - s0 > kSmallCell) {
-      if (q == s0) {
-        // at most n / (kSmallCell + 1) cells qualify, and big_cap is larger
-        const uint32_t w = atomicAdd(&a.ctrl->big_count, 1u);
-        if (w < a.big_cap) a.big_list[w] = k;
-      }
-    } else {
-      const uint32_t me = a.idx_tmp[q];
-      uint32_t rank = 0;
-      for (uint32_t m = s0; m < s1; ++m) rank += a.idx_tmp[m] < me ? 1u : 0u;
-      place_one(a, s0 + rank, me, k, overflow);
-    }
+  const uint32_t c0 = k < a.ncells ? a.cs_new[k] : 0u;
+  const uint32_t c1 = k < a.ncells ? a.cs_new[k + 1] : 0u;
+  // larger cells are the scan's work list, placed by k_cs_big
+  if (k < a.ncells && c1 - c0 <= kSmallCell) {
+    const uint32_t s1 = min(c1, min(total, a.n));
+    const uint32_t me = a.idx_tmp[q];
+    uint32_t rank = 0;
+    for (uint32_t m = c0; m < s1; ++m) rank += a.idx_tmp[m] < me ? 1u : 0u;
+    place_one(a, c0 + rank, me, k, overflow);
   }
   add_overflow(a, overflow);
 }

@@ -121,6 +121,8 @@ k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
   if (run_if && *run_if == 0u) return;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  // taking the tickets: the rebin's scan lists its large cells afresh
+  if (FINAL && count.ticket && i == 0) ctrl->big_count = 0u;
   const bool live = i < n;
   uint32_t flags = 0;
   float pen = 0.f, taking = 0.f, ke = 0.f, ke_plain = 0.f;

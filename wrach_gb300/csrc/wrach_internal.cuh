@@ -101,10 +101,12 @@ __device__ __forceinline__ int world_of_cell(const WorldDev* __restrict__ W,
 
 // Frame-time cell of one axis (assets/shaders/particles_per_cell.wgsl:14-27):
 // floor((p - anchor) / cell_size).  Out-of-grid and NaN inputs, undefined in
-// the WGSL, are clamped into the grid (NaN -> 0) and flagged.
+// the WGSL, are clamped into the grid (NaN -> 0) and flagged.  A quotient by
+// 1 is its dividend exactly, so cell size 1 skips the division.
 __device__ __forceinline__ uint32_t axis_cell(float p, float a, uint32_t cs,
                                               uint32_t g, uint32_t& flags) {
-  float f = floorf(__fdiv_rn(__fsub_rn(p, a), (float)cs));
+  const float d = __fsub_rn(p, a);
+  float f = floorf(cs == 1u ? d : __fdiv_rn(d, (float)cs));
   if (!(f >= 0.0f)) {
     flags |= (f != f) ? (kFlagNaN | kFlagOutOfGrid) : kFlagOutOfGrid;
     return 0u;
