@@ -68,3 +68,28 @@ def test_floor_pile(W, O):
     vel = rng.normal(0, 0.3, size=pos.shape).astype(np.float32)
     st = _run(W, O, dims, pos, vel, 1, 3, gravity=0.1)
     assert st["huge_cells"] == 0
+
+
+def test_profiled_frames_match_graph_frames(W, O):
+    # a profiled frame runs its launches one at a time on the frame's stream
+    # (the large cells' sort included); graph frames run that sort on a
+    # second stream beside the small cells' pass.  Both match the oracle.
+    dims = (64.0, 48.0)
+    pos, vel = _clustered(4, dims, [(10, 10, 300), (20, 20, 65), (30, 30, 64)], 2500)
+    sim = make_sim(W, dims, 1, 1, 4, 0.1, capacity=len(pos) + 16)
+    try:
+        w = O.world(dims[0], dims[1], 1)
+        ph = oracle_physics(O, 1, 4, 0.1)
+        sim.add_particles(pos, vel)
+        ref = O.pack(w, pos, vel, capacity=sim.capacity())
+        for f in range(6):
+            if f % 2 == 0:
+                ms = sim.profile_frame()
+                assert len(ms) == 8  # four Jacobi passes, four rebin launches
+                assert all(m >= 0.0 for m in ms)
+            else:
+                sim.step(1)
+            ref = O.step(w, ph, ref[0], ref[1], ref[2], 1)[:3]
+            assert_frame_equal(sim.read_frame(), ref, "frame %d" % (f + 1))
+    finally:
+        sim.close()
