@@ -1196,6 +1196,9 @@ int wrach_destroy(WrachContext* ctx) {
   {
     DeviceGuard guard(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    // a frame's work on `aux` is joined into `stream`, unless its enqueue
+    // failed between the fork and the join
+    if (ctx->aux) cudaStreamSynchronize(ctx->aux);
     release(ctx);
   }
   delete ctx;
