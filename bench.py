@@ -100,6 +100,16 @@ def ncu_traffic(kernel):
         return None
 
 
+def ncu_instructions(kernel):
+    """Warp instructions per launch of `kernel` from the committed ncu summary
+    (profiles/ncu_traffic.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f)["warp_instructions_per_launch"].get(kernel)
+    except Exception:
+        return None
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -360,6 +370,20 @@ def run_ours(args):
                "ms_per_step": 1000.0 * max_dt / args.e2e_steps}
 
     lattice = args.workload == "lattice"
+    clock_summary = clocks.summary()
+    # the Jacobi is bound by instruction issue: its warp instructions per
+    # launch (one ncu capture of this workload) over its live mean duration,
+    # against one instruction per scheduler per cycle on every SM
+    issue = None
+    inst = ncu_instructions(dom) if lattice else None
+    if inst and clock_summary.get("sm_max_mhz"):
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        ipeak = sms * 4 * clock_summary["sm_max_mhz"] * 1e6
+        issue = {"kernel": dom, "warp_instructions_per_launch": inst,
+                 "source": "profiles/ncu_traffic.json (ncu smsp__inst_executed.sum, one launch)",
+                 "achieved": inst / (dom_ms / 1000.0), "peak": ipeak,
+                 "peak_source": "%d SMs x 4 schedulers x %.0f MHz" % (sms, clock_summary["sm_max_mhz"]),
+                 "unit": "warp instructions/s", "frac": inst / (dom_ms / 1000.0) / ipeak}
     other = {"blobs": "particle-steps/s at 4M particles, clustered (plain CUDA step)",
              "reference": "particle-steps/s at 1M particles, the reference's own physics",
              "small": "particle-steps/s at 16K particles (plain CUDA step)"}
@@ -386,8 +410,9 @@ def run_ours(args):
         "rebin_steps_ms": rebin_steps,
         "trajectory": dict(phases, frames=args.trajectory,
                            note="frames of one pass; late frames are the collapsed floor"),
+        "issue_roofline": issue,
         "gpu_launches": launches,
-        "clocks": clocks.summary(),
+        "clocks": clock_summary,
         "e2e": e2e,
         "flags": sim.flags(),
     }
