@@ -1,0 +1,146 @@
+// Host-side state of a context and the helpers shared by the files of the C
+// ABI: context.cu (lifetime, uploads, frames, viewport streaming, readback)
+// and surrogate_host.cu (the learned surrogate).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/wrach.h"
+#include "wrach_kernels.h"
+
+namespace wrach {
+namespace host {
+
+// A world's device-resident particle store.
+struct Store {
+  float2* pos = nullptr;
+  float2* vel = nullptr;
+  uint32_t n = 0;
+  uint32_t cap = 0;
+};
+
+}  // namespace host
+}  // namespace wrach
+
+struct WrachContext {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // a frame's large-cell sort runs on `aux`, beside the small cells' pass
+  cudaStream_t aux = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  WrachConfig cfg{};
+  wrach::PhysDev ph{};
+  uint32_t nworlds = 0;
+  std::vector<wrach::WorldDev> worlds_h;
+  std::vector<uint32_t> cap_h;   // frame capacity per world
+  std::vector<uint32_t> n_h;     // frame particles per world
+  std::vector<uint32_t> poff_h;  // first frame particle of each world
+  uint32_t ncells = 0;
+  uint32_t total_cap = 0;
+  uint32_t n = 0;
+  uint32_t max_world_cells = 0;
+  wrach::WorldDev* worlds_d = nullptr;
+  float2 *pos = nullptr, *vel = nullptr, *pos_o = nullptr, *vel_o = nullptr;
+  float2 *q1 = nullptr, *q2 = nullptr;
+  uint32_t* cell_of[2] = {nullptr, nullptr};
+  uint32_t* cs[2] = {nullptr, nullptr};
+  int cur = 0;
+  uint32_t* keys = nullptr;
+  uint32_t *kA = nullptr, *kB = nullptr, *iA = nullptr, *iB = nullptr;
+  size_t sort_cap = 0;
+  uint32_t* hist = nullptr;
+  uint32_t* tile_sums = nullptr;  // one word per tile of the cell table
+  uint32_t ntiles = 0;
+  uint32_t* big_list = nullptr;               // counting sort: large-cell work list
+  uint32_t big_cap = 0;
+  int sms = 0;
+  uint32_t key_bits = 0, digit_bits = 0;
+  wrach::Ctrl* ctrl = nullptr;
+  int rebin_grid = 0;
+  std::vector<wrach::host::Store> stores;
+  float2 *stage_pos = nullptr, *stage_vel = nullptr;
+  size_t stage_cap = 0;
+  uint32_t* compact_sums = nullptr;   // viewport streaming: tile sums + 1 count word
+  size_t compact_cap = 0;
+  uint32_t* counts = nullptr;     // per-cell counts of the rebin (ncells + 1)
+  uint32_t* table_tmp = nullptr;  // one world's reference-layout table
+  uint32_t* gather_idx = nullptr; // nworlds + 1
+  uint32_t* gather_out = nullptr;
+  std::string err;
+  uint64_t launches = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  uint32_t graph_n[2] = {0, 0};       // particle count each graph was captured with
+  bool graph_ok = true;
+  uint32_t* render_cover = nullptr;   // wrach_render scratch and image
+  uint8_t* render_image = nullptr;
+  size_t render_cap = 0;
+  cudaEvent_t* event_hook = nullptr;  // wrach_profile_frame: one event per launch boundary
+  uint32_t event_count = 0;
+  // the learned surrogate (wrach_surrogate_*)
+  struct {
+    bool ready = false;
+    wrach::MlpDev m{};
+    float *params = nullptr, *grad = nullptr, *mom1 = nullptr, *mom2 = nullptr;
+    float *loss = nullptr, *metrics = nullptr;
+    float* part = nullptr;           // per-block metrics of a solve launch (8 floats a block)
+    wrach::GateState* gate = nullptr;
+    uint16_t* bf16 = nullptr;        // the six BF16 weight arrays
+    uint16_t* x = nullptr;           // features of the frame (capacity rows)
+    float2* corr = nullptr;          // the network's output (capacity)
+    uint16_t* tx = nullptr;          // training features (max_samples rows)
+    float2* tt = nullptr;            // training targets
+    uint32_t nsamples = 0, max_samples = 0, step = 0;
+    int blocks = 0;
+  } sur;
+};
+
+namespace wrach {
+namespace host {
+
+// Records `msg` as the context's last error and returns `code`.
+int fail(WrachContext* c, int code, const std::string& msg);
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+void dfree(void* p);
+
+// Makes `dev` current for the scope of a C ABI call.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int now = -1;
+    if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev)
+      cudaSetDevice(prev);
+  }
+};
+
+// The launch arguments of the context's current binned frame.
+wrach::SolveArgs solve_args(WrachContext* ctx);
+wrach::RebinArgs rebin_args(WrachContext* ctx);
+
+}  // namespace host
+}  // namespace wrach
+
+// Returns a status from the enclosing C ABI function (with `ctx` in scope)
+// when a CUDA call fails.
+#define CK(call)                                                             \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      return wrach::host::fail(ctx,                                          \
+                               e_ == cudaErrorMemoryAllocation               \
+                                   ? WRACH_ERR_OUT_OF_MEMORY                 \
+                                   : WRACH_ERR_CUDA,                         \
+                               std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
