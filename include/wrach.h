@@ -345,8 +345,11 @@ int wrach_surrogate_step(WrachContext *ctx, uint32_t nsteps,
 
 /* Runs one frame eagerly with a CUDA event between its kernel launches and
  * writes each launch's duration in milliseconds to ms[0 .. *count - 1]
- * (launch order: the solve launches, then the rebin).  Blocks.  No
- * counterpart in the reference (which has no GPU timers). */
+ * (launch order: the solve launches, then the rebin).  The launches run one
+ * at a time on the context's stream, including the large cells' sort, which
+ * wrach_step runs beside the small cells' pass.  Same results as
+ * wrach_step.  Blocks.  No counterpart in the reference (which has no GPU
+ * timers). */
 int wrach_profile_frame(WrachContext *ctx, float *ms, uint32_t cap,
                         uint32_t *count);
 
