@@ -6,9 +6,9 @@ assets/shaders/prefix_sum.wgsl:9-15) and lists changing them as a TODO
 (README.md:28).  Here the launch shape is a per-context setting, and `tune`
 picks it by timing candidates on the workload itself:
 
-  rebin_blocks   co-resident blocks of the rebin's radix-sort fallback (it
-                 runs only for cells beyond 8192 particles, so it is tuned
-                 only when candidates are passed)
+  rebin_blocks   the config's grid of the radix-sort rebin; frames use the
+                 counting sort, whose launches are sized by the particle and
+                 cell counts, so it is tuned only when candidates are passed
   solve_block    threads per block of the solve kernels
   cell_size      only when the caller allows it: it changes which particles
                  share a cell, hence the capacity rule and the summation order
