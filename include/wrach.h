@@ -46,6 +46,8 @@ extern "C" {
 #define WRACH_FLAG_OUT_OF_GRID 1u /* a key was clamped into the grid */
 #define WRACH_FLAG_NAN 2u         /* a non-finite position was binned */
 #define WRACH_FLAG_TIMEOUT 4u     /* a bounded device wait gave up */
+#define WRACH_FLAG_OVERFLOW 8u    /* particles did not fit the output
+                                     (wrach_pack_noalloc's status only) */
 
 /* The reference's 32-byte shader uniform, field for field
  * (runners/bevy/src/config_shader.rs:15-29, shaders/shared/src/lib.rs:19-31,
@@ -137,16 +139,23 @@ int wrach_add_particles_device(WrachContext *ctx, uint32_t world,
  * calls no allocating routine.  Its temporaries live in one static device
  * array sized for at most 131,072 particles and 524,288 grid cells (about
  * 6.3 MB on every GPU that loads the library, until exit); larger inputs
- * return WRACH_ERR_CAPACITY.  Particles past out_capacity are not written.
- * The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress), so make it before any stream capture.  Every call
- * shares the array: calls that overlap on the GPU race, so keep them on one
- * stream.  Asynchronous on `stream` (a cudaStream_t, NULL = the legacy
- * default stream).  No counterpart in the reference. */
+ * return WRACH_ERR_CAPACITY.  Particles past out_capacity are not written
+ * (d_indices still counts them).  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress), so make it before any
+ * stream capture.  Every call shares the array: calls that overlap on the GPU
+ * race, so keep them on one stream.  Asynchronous on `stream` (a
+ * cudaStream_t, NULL = the legacy default stream): the return code covers
+ * the arguments and the launches only.  What only the device knows goes to
+ * d_status (optional, NULL = not wanted; 2 u32 of device memory), written
+ * after the call's kernels: d_status[0] = WRACH_FLAG_* bits
+ * (WRACH_FLAG_TIMEOUT if a bounded grid barrier of the sort gave up, the
+ * output then being unreliable; WRACH_FLAG_OVERFLOW if particles did not fit
+ * out_capacity), d_status[1] = the number that did not fit.  No counterpart
+ * in the reference. */
 int wrach_pack_noalloc(const WrachConfig *config, const float *d_pos,
                        const float *d_vel, uint32_t n, float *d_pos_out,
                        float *d_vel_out, uint32_t out_capacity,
-                       uint32_t *d_indices, void *stream);
+                       uint32_t *d_indices, uint32_t *d_status, void *stream);
 
 /* nsteps frames of the physics pass list (builder.rs:86-89): solve, count,
  * scan, pack.  Asynchronous on the context's stream. */
@@ -242,13 +251,6 @@ int wrach_read_store(WrachContext *ctx, uint32_t world, float *positions,
 
 /* Reads the counters; blocks. */
 int wrach_stats(WrachContext *ctx, WrachStats *out);
-
-/* Phase trace of the latest radix-sort rebin (wrach_pack_noalloc's; frames
- * and uploads use the counting sort): %globaltimer (ns) at each phase
- * boundary, as recorded by its first block; *count receives the number of
- * entries (at most 32).  Blocks.  No counterpart in the reference. */
-int wrach_rebin_trace(WrachContext *ctx, uint64_t *ns, uint32_t cap,
-                      uint32_t *count);
 
 /* Self-test of the device's bounded wait, the one every device-side wait of
  * the library uses (grid barriers): a one-thread kernel waits on a device

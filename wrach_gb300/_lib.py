@@ -23,6 +23,7 @@ MODE_EXTENDED = 1
 FLAG_OUT_OF_GRID = 1
 FLAG_NAN = 2
 FLAG_TIMEOUT = 4
+FLAG_OVERFLOW = 8
 
 ERROR_NAMES = {
     1: "invalid argument", 2: "capacity exceeded", 3: "CUDA error",
@@ -98,7 +99,7 @@ SIGNATURES = {
     "wrach_profile_frame": (ctypes.c_int, [_P, _F, ctypes.c_uint32, _U]),
     "wrach_add_particles_device": (ctypes.c_int, [_P, ctypes.c_uint32, _P, _P, ctypes.c_uint32]),
     "wrach_pack_noalloc": (ctypes.c_int, [ctypes.POINTER(Config), _P, _P, ctypes.c_uint32, _P, _P,
-                                          ctypes.c_uint32, _P, _P]),
+                                          ctypes.c_uint32, _P, _P, _P]),
     "wrach_step": (ctypes.c_int, [_P, ctypes.c_uint32]),
     "wrach_read": (ctypes.c_int, [_P, ctypes.c_uint32, _F, _F, _U, ctypes.c_uint32]),
     "wrach_tick": (ctypes.c_int, [_P, ctypes.c_uint32, _F, _F, _U, ctypes.c_uint32]),
@@ -111,7 +112,6 @@ SIGNATURES = {
     "wrach_sync": (ctypes.c_int, [_P]),
     "wrach_flags": (ctypes.c_int, [_P, _U]),
     "wrach_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
-    "wrach_rebin_trace": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32, _U]),
     "wrach_last_error": (ctypes.c_char_p, [_P]),
     "wrach_kernel_launches": (ctypes.c_uint64, [_P]),
     "wrach_stream": (ctypes.c_void_p, [_P]),

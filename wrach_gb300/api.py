@@ -218,14 +218,6 @@ class Simulation:
         self._check(self._L.wrach_stats(self._ctx, ctypes.byref(st)))
         return {f: getattr(st, f) for f, _ in _lib.Stats._fields_ if f != "reserved"}
 
-    def rebin_trace(self):
-        """Nanoseconds between the phase boundaries of the latest rebin."""
-        buf = (ctypes.c_uint64 * 32)()
-        cnt = ctypes.c_uint32(0)
-        self._check(self._L.wrach_rebin_trace(self._ctx, buf, 32, ctypes.byref(cnt)))
-        t = [int(buf[i]) for i in range(cnt.value)]
-        return [b - a for a, b in zip(t, t[1:])]
-
     def frame_metrics(self):
         """(mean penetration, max penetration, kinetic energy) of the frame."""
         a, b, c = ctypes.c_float(0), ctypes.c_float(0), ctypes.c_float(0)

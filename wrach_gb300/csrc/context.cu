@@ -993,19 +993,6 @@ int wrach_stats(WrachContext* ctx, WrachStats* out) {
   return WRACH_OK;
 }
 
-int wrach_rebin_trace(WrachContext* ctx, uint64_t* ns, uint32_t cap, uint32_t* count) {
-  if (!ctx || !count) return WRACH_ERR_INVALID_ARGUMENT;
-  DeviceGuard guard(ctx->device);
-  Ctrl h{};
-  CK(cudaMemcpyAsync(&h, ctx->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  uint32_t n = 0;
-  while (n < wrach::kPhaseSlots && h.phase_ns[n]) ++n;
-  *count = n;
-  for (uint32_t i = 0; i < n && i < cap && ns; ++i) ns[i] = h.phase_ns[i];
-  return WRACH_OK;
-}
-
 const char* wrach_last_error(WrachContext* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
 uint64_t wrach_kernel_launches(WrachContext* ctx) { return ctx ? ctx->launches : 0; }

@@ -19,6 +19,11 @@
 // work; make it before any stream capture.  All calls share the one array,
 // so calls whose work overlaps on the GPU (other streams, other threads)
 // race with each other; serialise them on one stream.
+//
+// The call returns before its kernels run, so what can only be known on the
+// device (a grid barrier of the rebin that gave up, particles that did not
+// fit out_capacity) is written, once the kernels are done, to the caller's
+// optional two-word device status array.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -93,11 +98,16 @@ int32_t host_cell_coord(float x, uint32_t cs) {
   return (int32_t)q;
 }
 
+// Makes `dev` the current device for the lifetime of the object (ok is false
+// if that failed) and restores the caller's device afterwards.
 struct CurrentDevice {
   int prev = -1;
+  bool ok = false;
   explicit CurrentDevice(int dev) {
     if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    if (prev != dev) cudaSetDevice(dev);
+    if (prev != dev && cudaSetDevice(dev) != cudaSuccess) return;
+    int now = -1;
+    ok = cudaGetDevice(&now) == cudaSuccess && now == dev;
   }
   ~CurrentDevice() {
     int now = -1;
@@ -105,12 +115,34 @@ struct CurrentDevice {
   }
 };
 
+// The call's device-side outcome for the caller: status[0] = the WRACH_FLAG_*
+// bits the rebin raised (WRACH_FLAG_TIMEOUT: a grid barrier gave up), plus
+// WRACH_FLAG_OVERFLOW when particles did not fit out_capacity; status[1] =
+// how many did not fit.
+__global__ void k_noalloc_status(const Ctrl* __restrict__ ctrl, uint32_t* __restrict__ status) {
+  const uint32_t overflow = ctrl->overflow;
+  status[0] = ctrl->flags | (overflow ? WRACH_FLAG_OVERFLOW : 0u);
+  status[1] = overflow;
+}
+
+// One launch whose own return code is checked: an error left behind by the
+// caller's earlier CUDA calls is neither reported nor cleared here.
+template <typename... Params, typename... Args>
+cudaError_t launch(void (*kernel)(Params...), uint32_t blocks, uint32_t threads,
+                   cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(threads);
+  cfg.stream = st;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 }  // namespace
 
 extern "C" int wrach_pack_noalloc(const WrachConfig* config, const float* d_pos,
                                   const float* d_vel, uint32_t n, float* d_pos_out,
                                   float* d_vel_out, uint32_t out_capacity,
-                                  uint32_t* d_indices, void* stream) {
+                                  uint32_t* d_indices, uint32_t* d_status, void* stream) {
   if (!config || (n && (!d_pos || !d_vel)) || !d_pos_out || !d_vel_out || !d_indices)
     return WRACH_ERR_INVALID_ARGUMENT;
   if (config->cell_size == 0 || config->device < 0 ||
@@ -140,15 +172,14 @@ extern "C" int wrach_pack_noalloc(const WrachConfig* config, const float* d_pos,
   const uint32_t ncells = w.gx * w.gy;
 
   CurrentDevice current(config->device);
+  if (!current.ok) return WRACH_ERR_CUDA;  // the address below must be this device's
   uint32_t* base = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_scratch[config->device]) {
       void* ptr = nullptr;
-      if (cudaGetSymbolAddress(&ptr, wrach_noalloc_scratch) != cudaSuccess || !ptr) {
-        cudaGetLastError();
+      if (cudaGetSymbolAddress(&ptr, wrach_noalloc_scratch) != cudaSuccess || !ptr)
         return WRACH_ERR_CUDA;
-      }
       g_scratch[config->device] = static_cast<uint32_t*>(ptr);
     }
     base = g_scratch[config->device];
@@ -170,12 +201,9 @@ extern "C" int wrach_pack_noalloc(const WrachConfig* config, const float* d_pos,
       cudaMemsetAsync(base + kOffCounts, 0, ((size_t)ncells + 1) * 4, st) != cudaSuccess ||
       cudaMemsetAsync(d_indices, 0, 4, st) != cudaSuccess)
     return WRACH_ERR_CUDA;
-  if (n) {
-    k_noalloc_keys<<<(n + 255) / 256, 256, 0, st>>>(w, ncells, n,
-                                                   reinterpret_cast<const float2*>(d_pos),
-                                                   base + kOffKeys);
-    if (cudaGetLastError() != cudaSuccess) return WRACH_ERR_CUDA;
-  }
+  if (n && launch(k_noalloc_keys, (n + 255) / 256, 256, st, w, ncells, n,
+                  reinterpret_cast<const float2*>(d_pos), base + kOffKeys) != cudaSuccess)
+    return WRACH_ERR_CUDA;
 
   wrach::RebinArgs r{};
   r.worlds = nullptr;
@@ -201,9 +229,8 @@ extern "C" int wrach_pack_noalloc(const WrachConfig* config, const float* d_pos,
   r.force_general = 1;
   r.counts = base + kOffCounts;
   r.ctrl = reinterpret_cast<Ctrl*>(base + kOffCtrl);
-  if (wrach::launch_rebin(r, grid, st) != cudaSuccess) {
-    cudaGetLastError();
+  if (wrach::launch_rebin(r, grid, st) != cudaSuccess) return WRACH_ERR_CUDA;
+  if (d_status && launch(k_noalloc_status, 1, 1, st, r.ctrl, d_status) != cudaSuccess)
     return WRACH_ERR_CUDA;
-  }
   return WRACH_OK;
 }

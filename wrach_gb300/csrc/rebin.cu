@@ -101,13 +101,6 @@ __device__ void grid_barrier(Ctrl* ctrl, uint32_t& flags) {
 // loads of kSeg steps are issued before they are consumed.
 constexpr uint32_t kSeg = 8;
 
-// Phase trace: block 0 records the time at each phase boundary.
-__device__ __forceinline__ void trace(const RebinArgs& a, uint32_t& slot) {
-  if (blockIdx.x == 0 && threadIdx.x == 0 && slot < kPhaseSlots)
-    a.ctrl->phase_ns[slot] = global_ns();
-  ++slot;
-}
-
 // Sum of one tile of kTileCells per-cell counts (L2-coherent loads).
 __device__ __forceinline__ uint32_t tile_count_sum(const uint32_t* counts,
                                                    uint32_t tile, uint32_t n,
@@ -184,8 +177,6 @@ __device__ void radix_sort(const RebinArgs& a, SmemRebin& sm, uint32_t* wcd,
   const uint32_t ntiles = (a.ncells + kTileCells - 1) / kTileCells;
   uint32_t* tot = a.hist + RADIX * G;
   uint32_t* wc = wcd + warp * RADIX;
-  uint32_t slot = 0;
-  trace(a, slot);
 
   for (uint32_t p = 0; p < passes; ++p) {
     const uint32_t shift = DB * p;
@@ -221,9 +212,7 @@ __device__ void radix_sort(const RebinArgs& a, SmemRebin& sm, uint32_t* wcd,
       for (uint32_t w = 0; w < NW; ++w) h += wcd[w * RADIX + d];
       a.hist[d * G + b] = h;
     }
-    trace(a, slot);
     grid_barrier(a.ctrl, flags);
-    trace(a, slot);
 
     // B: per digit, exclusive prefix over the blocks and the digit total;
     // on the first pass also the tile sums of the per-cell counts
@@ -246,9 +235,7 @@ __device__ void radix_sort(const RebinArgs& a, SmemRebin& sm, uint32_t* wcd,
         const uint32_t s = tile_count_sum(a.counts, tile, a.ncells, sm);
         if (t == 0) a.tile_sums[tile] = s;
       }
-    trace(a, slot);
     grid_barrier(a.ctrl, flags);
-    trace(a, slot);
 
     // C: running destinations of each (warp, digit), then the stable scatter
     {
@@ -296,9 +283,7 @@ __device__ void radix_sort(const RebinArgs& a, SmemRebin& sm, uint32_t* wcd,
         __syncwarp();
       }
     }
-    trace(a, slot);
     grid_barrier(a.ctrl, flags);
-    trace(a, slot);
   }
 
   // gather into cell order, then the table
@@ -317,9 +302,7 @@ __device__ void radix_sort(const RebinArgs& a, SmemRebin& sm, uint32_t* wcd,
       ++overflow;
     }
   }
-  trace(a, slot);
   write_table(a, sm);
-  trace(a, slot);
 }
 
 __global__ void __launch_bounds__(T, 3) k_rebin(RebinArgs a) {

@@ -52,11 +52,7 @@ struct Ctrl {
   uint32_t big_count;   // counting sort: cells on the large-cell work list
   uint32_t huge_cells;  // counting sort: cells sorted in global memory, since create
   uint32_t pad[6];
-  // %globaltimer at the phase boundaries of the latest rebin launch, taken
-  // by block 0 (phase trace; kPhaseSlots entries, unused ones zero)
-  uint64_t phase_ns[32];
 };
-constexpr uint32_t kPhaseSlots = 32;
 
 constexpr uint32_t kFlagOutOfGrid = 1u;
 constexpr uint32_t kFlagNaN = 2u;
