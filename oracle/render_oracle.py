@@ -5,8 +5,9 @@ half-size 0.4 world units per particle, white on black, MSAA 4
 (runners/bevy/src/render/pipeline.rs:52-56).  Pixel coordinates
 X = x * sx, Y = height_px - y * sy (sx = width_px / W, sy = height_px / H);
 a particle covers [X - hx, X + hx) x [Y - hy, Y + hy), hx = 0.4 sx,
-hy = 0.4 sy; the four standard sample positions per pixel; value =
-255 * (most covered samples of one particle) // 4.
+hy = 0.4 sy; the four standard sample positions per pixel.  A multisampled
+target turns a sample white once any quad covers it, so a pixel resolves to
+255 * (samples covered by the union of the quads) // 4.
 """
 import numpy as np
 
@@ -30,6 +31,7 @@ def render(pos, world_w, world_h, width_px, height_px):
             for px in range(max(int(np.floor(x0)), 0), min(int(np.floor(x1)), width_px - 1) + 1):
                 s_x = (f(px) + SX).astype(np.float32)
                 s_y = (f(py) + SY).astype(np.float32)
-                c = int(np.sum((s_x >= x0) & (s_x < x1) & (s_y >= y0) & (s_y < y1)))
-                cover[py, px] = max(cover[py, px], c)
-    return (255 * cover // 4).astype(np.uint8)
+                hit = (s_x >= x0) & (s_x < x1) & (s_y >= y0) & (s_y < y1)
+                cover[py, px] |= int(np.sum(hit.astype(np.uint32) << np.arange(4, dtype=np.uint32)))
+    samples = sum((cover >> k) & 1 for k in range(4))
+    return (255 * samples // 4).astype(np.uint8)

@@ -10,8 +10,11 @@
 // A particle covers the axis-aligned square [X - hx, X + hx) x [Y - hy, Y + hy)
 // with hx = 0.4 * sx, hy = 0.4 * sy; a sample is covered when it lies in that
 // half-open square (the top-left fill rule of an axis-aligned quad).  Each
-// pixel has the four standard MSAA sample positions; its value is
-// 255 * (covered samples of the most-covering particle) / 4, rounded down.
+// pixel has the four standard MSAA sample positions.  As in a multisampled
+// colour target, a sample is white once any quad covers it, so a pixel's
+// value is the resolve of the union of its covered samples:
+// 255 * popcount(mask) / 4, rounded down, where the 4-bit mask is OR-ed over
+// every particle that touches the pixel.
 #include <stdint.h>
 
 #include "wrach_internal.cuh"
@@ -40,21 +43,21 @@ __global__ void k_raster(const float2* __restrict__ pos, uint32_t n, float sx, f
   const int py0 = max((int)floorf(y0), 0), py1 = min((int)floorf(y1), (int)height_px - 1);
   for (int py = py0; py <= py1; ++py)
     for (int px = px0; px <= px1; ++px) {
-      uint32_t c = 0;
+      uint32_t mask = 0;
 #pragma unroll
       for (int s = 0; s < 4; ++s) {
         const float sxp = __fadd_rn((float)px, kSampleX[s]);
         const float syp = __fadd_rn((float)py, kSampleY[s]);
-        c += (sxp >= x0 && sxp < x1 && syp >= y0 && syp < y1);
+        mask |= (sxp >= x0 && sxp < x1 && syp >= y0 && syp < y1) ? 1u << s : 0u;
       }
-      if (c) atomicMax(&cover[(size_t)py * width_px + px], c);
+      if (mask) atomicOr(&cover[(size_t)py * width_px + px], mask);
     }
 }
 
 __global__ void k_resolve(const uint32_t* __restrict__ cover, size_t npix,
                           uint8_t* __restrict__ image) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < npix) image[i] = (uint8_t)(255u * cover[i] / 4u);
+  if (i < npix) image[i] = (uint8_t)(255u * (uint32_t)__popc(cover[i]) / 4u);
 }
 
 }  // namespace
