@@ -78,8 +78,8 @@ typedef struct WrachConfig {
                               default 9 */
   uint32_t capacity;       /* 0 = max_particles_per_frame of the grid */
   int32_t device;          /* CUDA ordinal (default 0) */
-  uint32_t rebin_blocks;   /* blocks of the radix-sort rebin (allocation-free
-                              packing), 0 = all that fit */
+  uint32_t rebin_blocks;   /* blocks of the rebin's large-cell sort (cells of
+                              more than 64 particles), 0 = 8 per SM */
   uint32_t solve_block;    /* threads per block of the solve kernels, a
                               multiple of 32 up to 512, 0 = 128 */
   uint32_t reserved[5];
@@ -210,7 +210,7 @@ typedef struct WrachStats {
   uint32_t flags;             /* sticky WRACH_FLAG_* bits */
   uint32_t frames;            /* frames stepped since create */
   uint32_t overflow;          /* particles without destination room */
-  uint32_t rebin_blocks;      /* co-resident blocks of the radix-sort rebin */
+  uint32_t rebin_blocks;      /* blocks of the rebin's large-cell sort */
   uint32_t tiles;             /* tiles of the cell table */
   uint32_t particles;         /* particles in the frame, all worlds */
   uint32_t cells;             /* grid cells, all worlds */

@@ -63,3 +63,38 @@ def test_reference_arm_on_rank_1_does_no_work():
                         "--steps", "1", "--warmup", "0"], cwd=ROOT, env=env,
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def _batch_rank_main(rank, port, out):
+    """One rank of `bench.py --workload batch` with the GPU replaced by a CPU
+    stand-in: the rank takes its worlds through bench.batch_worlds (the
+    bench's own sharding) and "steps" them by counting their particles."""
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    sys.path.insert(0, ROOT)
+    import bench
+    torch.distributed.init_process_group("gloo", rank=rank, world_size=2)
+    try:
+        lo, hi, dims, poss, vels = bench.batch_worlds(rank, 2)
+        assert len(dims) == len(poss) == len(vels) == hi - lo
+        sizes = [len(p) for p in poss]
+        _, units = replicas.aggregate(1.0, float(sum(sizes)))
+        out[rank] = (lo, hi, sizes, units)
+    finally:
+        torch.distributed.destroy_process_group()
+
+
+def test_batch_worlds_shard_over_two_gloo_ranks():
+    """Unmeasured on hardware (one GPU per run here): every one of the 256
+    worlds is stepped by exactly one rank, and the ranks' units add up to
+    the whole batch."""
+    from wrach_gb300 import workloads
+    _, all_pos, _ = workloads.batch()
+    port = _free_port()
+    with mp.get_context("spawn").Manager() as m:
+        out = m.dict()
+        mp.start_processes(_batch_rank_main, args=(port, out), nprocs=2, start_method="spawn")
+        (lo0, hi0, s0, u0), (lo1, hi1, s1, u1) = out[0], out[1]
+    assert (lo0, hi0, lo1, hi1) == (0, 128, 128, 256)
+    assert s0 + s1 == [len(p) for p in all_pos]
+    assert u0 == u1 == float(sum(len(p) for p in all_pos))

@@ -6,14 +6,17 @@ assets/shaders/prefix_sum.wgsl:9-15) and lists changing them as a TODO
 (README.md:28).  Here the launch shape is a per-context setting, and `tune`
 picks it by timing candidates on the workload itself:
 
-  rebin_blocks   the config's grid of the radix-sort rebin; frames use the
-                 counting sort, whose launches are sized by the particle and
-                 cell counts, so it is tuned only when candidates are passed
   solve_block    threads per block of the solve kernels
-  cell_size      only when the caller allows it: it changes which particles
+  rebin_blocks   the grid of the rebin's large-cell sort (its blocks loop
+                 over the cells of more than 64 particles; default 8 per SM)
+  cell_size      only when the caller passes `cell_sizes`: it is a physics
+                 change, not a launch shape -- it changes which particles
                  share a cell, hence the capacity rule and the summation order
                  (results stay deterministic but are not those of another cell
                  size)
+
+A launch shape never changes results: every candidate steps the same frames
+bit for bit.
 
 Results are cached as JSON, keyed by GPU name and the workload's shape, so
 later runs skip the timing.
@@ -89,19 +92,28 @@ def _time_frames(sim, frames):
     return (time.perf_counter() - t0) * 1000.0 / frames
 
 
+LAUNCH_KNOBS = ("solve_block", "rebin_blocks")
+
+
+def launch_shape(config):
+    """The tuned knobs of a config (cell size included)."""
+    return {k: getattr(config, k) for k in ("cell_size",) + LAUNCH_KNOBS}
+
+
 def tune(config, positions, velocities, worlds=None, frames=10, rebin_blocks=None,
          solve_blocks=(128, 256, 512), cell_sizes=None, use_cache=True, path=None):
     """Returns (tuned config, {candidate: ms per frame}).  `positions` and
     `velocities` are one (n, 2) array each, or one per world when `worlds`
-    (a list of (width, height)) is given.  `cell_sizes` (e.g. (1, 2)) lets the
-    tuner change the cell size."""
+    (a list of (width, height)) is given.  `rebin_blocks` defaults to 4, 8
+    and 16 blocks per SM.  `cell_sizes` (e.g. (1, 2)) lets the tuner change
+    the cell size, which changes the physics."""
     tune_cs = bool(cell_sizes)
     cell_sizes = tuple(cell_sizes) if cell_sizes else (config.cell_size,)
     probe = api.Simulation(dataclasses.replace(config), worlds=worlds)
     try:
         stats = probe.stats()
         particles = sum(len(p) for p in positions) if worlds is not None else len(positions)
-        max_blocks = stats["rebin_blocks"]
+        per_sm8 = stats["rebin_blocks"]  # the default: 8 blocks per SM
         key = workload_key(_gpu_name(), config, probe.num_worlds, particles, stats["cells"], tune_cs)
     finally:
         probe.close()
@@ -109,7 +121,7 @@ def tune(config, positions, velocities, worlds=None, frames=10, rebin_blocks=Non
     if use_cache and key in cache:
         return dataclasses.replace(config, **cache[key]["choice"]), cache[key]["ms"]
     if rebin_blocks is None:
-        rebin_blocks = (max_blocks,)
+        rebin_blocks = (per_sm8 // 2, per_sm8, per_sm8 * 2)
     timings = {}
     best, best_ms = None, float("inf")
     for cs in cell_sizes:

@@ -14,7 +14,6 @@
 //   keys              next cell of each solve output (u32)
 //   kA kB iA iB       rebin scratch (tickets, slot cells, slot sources, sort ping-pong)
 //   tile_sums         rebin: particles per tile of 2048 cells (zero between frames)
-//   hist              radix-sort scratch (wrach_pack_noalloc's sort)
 //   ctrl              counters and sticky flags
 #include <algorithm>
 #include <cmath>
@@ -97,7 +96,7 @@ void release(WrachContext* ctx) {
   void* ptrs[] = {ctx->worlds_d, ctx->pos, ctx->vel, ctx->pos_o, ctx->vel_o,
                   ctx->q1, ctx->q2, ctx->cell_of[0], ctx->cell_of[1],
                   ctx->cs[0], ctx->cs[1], ctx->keys, ctx->kA, ctx->kB,
-                  ctx->iA, ctx->iB, ctx->hist, ctx->tile_sums, ctx->ctrl, ctx->big_list,
+                  ctx->iA, ctx->iB, ctx->tile_sums, ctx->ctrl, ctx->big_list,
                   ctx->stage_pos, ctx->stage_vel, ctx->table_tmp, ctx->counts, ctx->render_cover, ctx->render_image,
                   ctx->gather_idx, ctx->gather_out, ctx->compact_sums};
   for (void* p : ptrs) dfree(p);
@@ -205,9 +204,6 @@ wrach::RebinArgs rebin_args(WrachContext* ctx) {
   r.kB = ctx->kB;
   r.iA = ctx->iA;
   r.iB = ctx->iB;
-  r.hist = ctx->hist;
-  r.key_bits = ctx->key_bits;
-  r.digit_bits = ctx->digit_bits;
   r.keys = ctx->keys;
   r.counts = ctx->counts;
   r.ctrl = ctx->ctrl;
@@ -281,13 +277,13 @@ int enqueue_frame(WrachContext* ctx) {
     if (fork && step == wrach::kCountSortSteps - 2) {
       CK(cudaEventRecord(ctx->fork_ev, st));
       CK(cudaStreamWaitEvent(ctx->aux, ctx->fork_ev, 0));
-      CK(wrach::launch_count_sort_step(r, step + 1, ctx->sms, ctx->aux, &launched));
+      CK(wrach::launch_count_sort_step(r, step + 1, ctx->big_blocks, ctx->aux, &launched));
       CK(cudaEventRecord(ctx->join_ev, ctx->aux));
-      CK(wrach::launch_count_sort_step(r, step, ctx->sms, st, &launched));
+      CK(wrach::launch_count_sort_step(r, step, ctx->big_blocks, st, &launched));
       CK(cudaStreamWaitEvent(st, ctx->join_ev, 0));
       break;
     }
-    CK(wrach::launch_count_sort_step(r, step, ctx->sms, st, &launched));
+    CK(wrach::launch_count_sort_step(r, step, ctx->big_blocks, st, &launched));
     if (launched) mark(ctx);
   }
   ctx->launches += wrach::count_sort_launches(r.n) - (tickets_taken && r.n ? 1 : 0);
@@ -441,15 +437,6 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   }
   ctx->ncells = (uint32_t)cells;
   ctx->total_cap = (uint32_t)cap;
-  ctx->key_bits = bits_for(ctx->ncells);
-  ctx->digit_bits = wrach::rebin_digit_bits(ctx->key_bits);
-  ctx->rebin_grid = wrach::rebin_grid_size(ctx->device, ctx->digit_bits);
-  if (c.rebin_blocks && (int)c.rebin_blocks < ctx->rebin_grid) ctx->rebin_grid = (int)c.rebin_blocks;
-  if (ctx->rebin_grid <= 0) {
-    int rc = fail(ctx, WRACH_ERR_CUDA, "cannot size the rebin grid (kernel image not loadable?)");
-    delete ctx;
-    return rc;
-  }
 
   auto oom = [&](cudaError_t e) {
     int rc = fail(ctx, e == cudaErrorMemoryAllocation ? WRACH_ERR_OUT_OF_MEMORY : WRACH_ERR_CUDA,
@@ -486,8 +473,6 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
     if ((e = dalloc(&ctx->cs[i], (size_t)ctx->ncells + 1)) != cudaSuccess) return oom(e);
     if ((e = cudaMemset(ctx->cs[i], 0, ((size_t)ctx->ncells + 1) * 4)) != cudaSuccess) return oom(e);
   }
-  if ((e = dalloc(&ctx->hist, ((size_t)1 << ctx->digit_bits) * (ctx->rebin_grid + 1))) != cudaSuccess)
-    return oom(e);
   // one sum per tile of kTileCells cells of the table
   ctx->ntiles = (ctx->ncells + wrach::kTileCells - 1) / wrach::kTileCells;
   if ((e = dalloc(&ctx->tile_sums, ctx->ntiles)) != cudaSuccess) return oom(e);
@@ -496,6 +481,7 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   if ((e = cudaMemset(ctx->tile_sums, 0, (size_t)ctx->ntiles * 4)) != cudaSuccess) return oom(e);
   if ((e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device)) != cudaSuccess)
     return oom(e);
+  ctx->big_blocks = c.rebin_blocks ? c.rebin_blocks : wrach::kBigBlocksPerSm * (uint32_t)ctx->sms;
   if ((e = dalloc(&ctx->ctrl, 1)) != cudaSuccess) return oom(e);
   if ((e = cudaMemset(ctx->ctrl, 0, sizeof(Ctrl))) != cudaSuccess) return oom(e);
   if ((e = dalloc(&ctx->table_tmp, (size_t)ctx->max_world_cells + 2)) != cudaSuccess) return oom(e);
@@ -591,7 +577,7 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
   r.vel_dst = ctx->vel_o;
   r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
   r.force_general = 1;
-  CK(wrach::launch_count_sort(r, ctx->sms, ctx->stream));
+  CK(wrach::launch_count_sort(r, ctx->big_blocks, ctx->stream));
   ctx->launches += wrach::count_sort_launches(r.n);
 
   // per-world counts from the new table
@@ -985,7 +971,7 @@ int wrach_stats(WrachContext* ctx, WrachStats* out) {
   out->flags = h.flags;
   out->frames = h.frames;
   out->overflow = h.overflow;
-  out->rebin_blocks = (uint32_t)ctx->rebin_grid;
+  out->rebin_blocks = ctx->big_blocks;
   out->tiles = ctx->ntiles;
   out->particles = ctx->n;
   out->cells = ctx->ncells;

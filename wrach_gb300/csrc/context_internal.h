@@ -50,15 +50,13 @@ struct WrachContext {
   uint32_t* keys = nullptr;
   uint32_t *kA = nullptr, *kB = nullptr, *iA = nullptr, *iB = nullptr;
   size_t sort_cap = 0;
-  uint32_t* hist = nullptr;
   uint32_t* tile_sums = nullptr;  // one word per tile of the cell table
   uint32_t ntiles = 0;
   uint32_t* big_list = nullptr;               // counting sort: large-cell work list
   uint32_t big_cap = 0;
   int sms = 0;
-  uint32_t key_bits = 0, digit_bits = 0;
   wrach::Ctrl* ctrl = nullptr;
-  int rebin_grid = 0;
+  uint32_t big_blocks = 0;  // grid of the rebin's large-cell sort
   std::vector<wrach::host::Store> stores;
   float2 *stage_pos = nullptr, *stage_vel = nullptr;
   size_t stage_cap = 0;

@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(256) k_cs_place(RebinArgs a) {
   add_overflow(a, overflow);
 }
 
-constexpr uint32_t kBigThreads = 256, kBigBlocksPerSm = 8;
+constexpr uint32_t kBigThreads = 256;
 static_assert(kBigThreads == 256, "one radix digit per thread");
 
 // Stable block-wide LSD radix sort (8-bit digits) of the m values src[0..m)
@@ -304,8 +304,8 @@ __global__ void __launch_bounds__(kBigThreads) k_cs_big(RebinArgs a) {
 
 }  // namespace
 
-cudaError_t launch_count_sort_step(const RebinArgs& a, int step, int sms, cudaStream_t st,
-                                   bool* launched) {
+cudaError_t launch_count_sort_step(const RebinArgs& a, int step, uint32_t big_blocks,
+                                   cudaStream_t st, bool* launched) {
   const uint32_t ntiles = (a.ncells + kScanTile - 1) / kScanTile;
   const uint32_t nblk = (a.n + 255) / 256;
   *launched = true;
@@ -325,15 +325,15 @@ cudaError_t launch_count_sort_step(const RebinArgs& a, int step, int sms, cudaSt
   } else if (step == 3) {
     k_cs_place<<<nblk, 256, 0, st>>>(a);
   } else {
-    k_cs_big<<<(sms > 0 ? sms : 1) * kBigBlocksPerSm, kBigThreads, 0, st>>>(a);
+    k_cs_big<<<big_blocks ? big_blocks : 1u, kBigThreads, 0, st>>>(a);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_count_sort(const RebinArgs& a, int sms, cudaStream_t st) {
+cudaError_t launch_count_sort(const RebinArgs& a, uint32_t big_blocks, cudaStream_t st) {
   for (int step = 0; step < kCountSortSteps; ++step) {
     bool launched;
-    const cudaError_t e = launch_count_sort_step(a, step, sms, st, &launched);
+    const cudaError_t e = launch_count_sort_step(a, step, big_blocks, st, &launched);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

@@ -90,14 +90,17 @@ constexpr uint32_t kCountScanShift = 11;
 constexpr uint32_t kCountScanTile = 1u << kCountScanShift;  // cells per scan tile (tile_sums entry)
 constexpr uint32_t kSmallCell = 64;
 constexpr uint32_t kBigCell = 2048;
-cudaError_t launch_count_sort(const RebinArgs& a, int sms, cudaStream_t st);
+// big_blocks: the grid of the large-cell step (its blocks loop over the
+// listed cells); kBigBlocksPerSm per SM unless a config sets it.
+constexpr uint32_t kBigBlocksPerSm = 8;
+cudaError_t launch_count_sort(const RebinArgs& a, uint32_t big_blocks, cudaStream_t st);
 // The same, one step at a time (steps 0 .. kCountSortSteps - 1: count, scan,
 // scatter, place, large cells); *launched is false for a step that has
 // nothing to do.  Step 0 may be left out when the tickets were taken by the
 // last Jacobi pass (SolveArgs::count).
 constexpr int kCountSortSteps = 5;
-cudaError_t launch_count_sort_step(const RebinArgs& a, int step, int sms, cudaStream_t st,
-                                   bool* launched);
+cudaError_t launch_count_sort_step(const RebinArgs& a, int step, uint32_t big_blocks,
+                                   cudaStream_t st, bool* launched);
 uint32_t count_sort_launches(uint32_t n);
 
 // Keys for an upload re-pack: the first n_keep sources are particles of the
