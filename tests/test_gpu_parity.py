@@ -208,6 +208,48 @@ def test_batched_worlds_match_single_world_oracle(W, O):
         sim.close()
 
 
+@pytest.mark.parametrize("cell_size", [1, 2])
+def test_batch_256_worlds_checked_every_100_steps(W, O, cell_size):
+    # the full batched-worlds workload: 256 worlds (sides U[128, 1024],
+    # counts log-uniform in [1024, 65536], 3.85 M particles), extended
+    # physics, 500 steps, at the configured cell size 1 and the tuned 2.
+    # Every 100 steps the GPU state of 8 worlds (the smallest, the largest, 6
+    # at random) is stepped once by the single-world oracle (the per-world
+    # semantics of spatial_bin.rs:103-149, cell.rs:52-95) and the next GPU
+    # frame of each (table, order, positions, velocities) must match
+    from wrach_gb300 import workloads
+    dims, poss, vels = workloads.batch()
+    sizes = [len(p) for p in poss]
+    cfg = W.WrachConfig(cell_size=cell_size, mode=1, iterations=4, gravity=0.1,
+                        capacity=int(max(sizes)))
+    sim = W.Simulation(cfg, worlds=dims.tolist())
+    try:
+        rng = np.random.default_rng(3)
+        sample = sorted({int(np.argmin(sizes)), int(np.argmax(sizes))}
+                        | set(int(k) for k in rng.choice(len(poss), 6, replace=False)))
+        for k, (p, v) in enumerate(zip(poss, vels)):
+            sim.set_particles(p, v, world=k)
+        ph = O.extended_physics(4, 0.1)
+        worlds = {k: O.world(float(dims[k][0]), float(dims[k][1]), cell_size) for k in sample}
+        for k in sample:
+            ref = O.pack(worlds[k], poss[k], vels[k], sim.capacity(k))
+            assert_frame_equal(sim.read_frame(k), ref, "world %d upload" % k)
+        done = 0
+        while done < 500:
+            sim.step(99)
+            states = {k: sim.read_frame(k) for k in sample}
+            sim.step(1)
+            done += 100
+            for k in sample:
+                gp, gv, gt = states[k]
+                want = O.step(worlds[k], ph, gt, gp, gv, 1)[:3]
+                assert_frame_equal(sim.read_frame(k), want, "world %d step %d" % (k, done))
+                assert int(gt[-1]) == sizes[k]
+        assert sim.stats()["overflow"] == 0
+    finally:
+        sim.close()
+
+
 @pytest.mark.parametrize("mode", [0, 1])
 def test_full_size_lattice_steps(W, O, mode):
     # 1,000,000 particles, 1920x1080, cell 1: the benchmark workload

@@ -11,6 +11,10 @@
 //   q1, q2            extended-mode Jacobi iterates
 //   cell_of[2]        cell of each binned particle (u32)
 //   cs[2]             cell-start table, cells + 1 u32 (ping-pong per frame)
+//   ct[2], tp_pos[2], tp_cell[2]
+//                     extended physics: the capped table (start of each
+//                     cell's taking-part particles among them all) and those
+//                     particles' positions and cells, compacted in cell order
 //   keys              next cell of each solve output (u32)
 //   kA kB iA iB       rebin scratch (tickets, slot cells, slot sources, sort ping-pong)
 //   tile_sums         rebin: particles per tile of 2048 cells (zero between frames)
@@ -97,6 +101,8 @@ void release(WrachContext* ctx) {
                   ctx->q1, ctx->q2, ctx->cell_of[0], ctx->cell_of[1],
                   ctx->cs[0], ctx->cs[1], ctx->keys, ctx->kA, ctx->kB,
                   ctx->iA, ctx->iB, ctx->tile_sums, ctx->ctrl, ctx->big_list,
+                  ctx->ct[0], ctx->ct[1], ctx->tp_pos[0], ctx->tp_pos[1], ctx->tp_cell[0],
+                  ctx->tp_cell[1], ctx->tile_sums_cap,
                   ctx->stage_pos, ctx->stage_vel, ctx->table_tmp, ctx->counts, ctx->render_cover, ctx->render_image,
                   ctx->gather_idx, ctx->gather_out, ctx->compact_sums};
   for (void* p : ptrs) dfree(p);
@@ -191,7 +197,15 @@ wrach::SolveArgs solve_args(WrachContext* ctx) {
   a.keys = ctx->keys;
   a.ctrl = ctx->ctrl;
   a.block = ctx->cfg.solve_block;
+  a.ct = ctx->ct[ctx->cur];
+  a.tp_cell = ctx->tp_cell[ctx->cur];
+  a.tp_pos = ctx->tp_pos[ctx->cur];
   return a;
+}
+
+wrach::CountDev ticket_args(WrachContext* ctx) {
+  return wrach::CountDev{ctx->counts, ctx->tile_sums, ctx->kA, ctx->ncells, wrach::kCountScanShift,
+                         ctx->ph.cap, ctx->tile_sums_cap};
 }
 
 wrach::RebinArgs rebin_args(WrachContext* ctx) {
@@ -213,6 +227,15 @@ wrach::RebinArgs rebin_args(WrachContext* ctx) {
   r.idx_alt = ctx->iB;
   r.big_list = ctx->big_list;
   r.big_cap = ctx->big_cap;
+  // every rebin writes the next table parity; extended physics also the
+  // compacted taking-part particles
+  if (ctx->ph.mode == WRACH_MODE_EXTENDED) {
+    r.tp_cap = ctx->ph.cap;
+    r.tile_sums_cap = ctx->tile_sums_cap;
+    r.ct_new = ctx->ct[ctx->cur ^ 1];
+    r.tp_pos = ctx->tp_pos[ctx->cur ^ 1];
+    r.tp_cell = ctx->tp_cell[ctx->cur ^ 1];
+  }
   return r;
 }
 
@@ -237,25 +260,13 @@ int enqueue_frame(WrachContext* ctx) {
   } else {
     // the last pass takes the rebin's tickets (it computes the keys)
     wrach::SolveArgs fin = a;
-    fin.count = wrach::CountDev{ctx->counts, ctx->tile_sums, ctx->kA, ctx->ncells,
-                                wrach::kCountScanShift};
+    fin.count = ticket_args(ctx);
     const uint32_t K = ctx->ph.iterations;
-    if (K == 0) {
-      CK(wrach::launch_solve_extended(fin, ctx->pos, ctx->pos_o, true, 0, st));
-      mark(ctx);
-      ctx->launches += 1;
-    } else {
-      const float2* src = ctx->pos;
-      for (uint32_t it = 0; it + 1 < K; ++it) {
-        float2* dst = (it & 1) ? ctx->q2 : ctx->q1;
-        CK(wrach::launch_solve_extended(a, src, dst, false, 1, st));
-        mark(ctx);
-        src = dst;
-      }
-      CK(wrach::launch_solve_extended(fin, src, ctx->pos_o, true, 1, st));
-      mark(ctx);
-      ctx->launches += K;
-    }
+    const float2* q = nullptr;
+    CK(enqueue_iterations(ctx, a, K > 0 ? K - 1 : 0, st, &q, [&]() { mark(ctx); }));
+    CK(wrach::launch_jacobi_final(fin, q, K > 0 ? 1 : 0, st));
+    mark(ctx);
+    ctx->launches += std::max<uint32_t>(K, 1);
   }
   const bool tickets_taken = ctx->ph.mode != WRACH_MODE_REFERENCE;
   wrach::RebinArgs r = rebin_args(ctx);
@@ -468,6 +479,14 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
     if ((e = dalloc(&ctx->q1, tc)) != cudaSuccess) return oom(e);
     if ((e = dalloc(&ctx->q2, tc)) != cudaSuccess) return oom(e);
   }
+  if (c.mode == WRACH_MODE_EXTENDED) {
+    for (int i = 0; i < 2; ++i) {
+      if ((e = dalloc(&ctx->ct[i], (size_t)ctx->ncells + 1)) != cudaSuccess) return oom(e);
+      if ((e = cudaMemset(ctx->ct[i], 0, ((size_t)ctx->ncells + 1) * 4)) != cudaSuccess) return oom(e);
+      if ((e = dalloc(&ctx->tp_pos[i], tc)) != cudaSuccess) return oom(e);
+      if ((e = dalloc(&ctx->tp_cell[i], tc)) != cudaSuccess) return oom(e);
+    }
+  }
   for (int i = 0; i < 2; ++i) {
     if ((e = dalloc(&ctx->cell_of[i], tc)) != cudaSuccess) return oom(e);
     if ((e = dalloc(&ctx->cs[i], (size_t)ctx->ncells + 1)) != cudaSuccess) return oom(e);
@@ -479,6 +498,10 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   // the counting sort's tile sums reuse the table tile sums (kTileCells <= 2048)
   static_assert(wrach::kTileCells <= wrach::kCountScanTile, "tile sums buffer large enough");
   if ((e = cudaMemset(ctx->tile_sums, 0, (size_t)ctx->ntiles * 4)) != cudaSuccess) return oom(e);
+  if (c.mode == WRACH_MODE_EXTENDED) {
+    if ((e = dalloc(&ctx->tile_sums_cap, ctx->ntiles)) != cudaSuccess) return oom(e);
+    if ((e = cudaMemset(ctx->tile_sums_cap, 0, (size_t)ctx->ntiles * 4)) != cudaSuccess) return oom(e);
+  }
   if ((e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device)) != cudaSuccess)
     return oom(e);
   ctx->big_blocks = c.rebin_blocks ? c.rebin_blocks : wrach::kBigBlocksPerSm * (uint32_t)ctx->sms;

@@ -51,6 +51,11 @@ struct WrachContext {
   uint32_t *kA = nullptr, *kB = nullptr, *iA = nullptr, *iB = nullptr;
   size_t sort_cap = 0;
   uint32_t* tile_sums = nullptr;  // one word per tile of the cell table
+  // extended physics: the taking-part particles compacted (ping-pong with cs)
+  uint32_t* ct[2] = {nullptr, nullptr};       // capped table, cells + 1
+  float2* tp_pos[2] = {nullptr, nullptr};     // compacted positions
+  uint32_t* tp_cell[2] = {nullptr, nullptr};  // compacted cells
+  uint32_t* tile_sums_cap = nullptr;          // per scan tile, taking-part particles
   uint32_t ntiles = 0;
   uint32_t* big_list = nullptr;               // counting sort: large-cell work list
   uint32_t big_cap = 0;
@@ -126,6 +131,27 @@ struct DeviceGuard {
 // The launch arguments of the context's current binned frame.
 wrach::SolveArgs solve_args(WrachContext* ctx);
 wrach::RebinArgs rebin_args(WrachContext* ctx);
+// What a frame's last extended pass needs to take the rebin's tickets.
+wrach::CountDev ticket_args(WrachContext* ctx);
+
+// The first `count` extended iterations of the binned frame over the
+// compacted taking-part particles, from a.tp_pos through the iterates q1 and
+// q2 in turn; *q receives the last iterate (a.tp_pos when count is 0).
+// `after` runs after each launch.
+template <typename After>
+cudaError_t enqueue_iterations(WrachContext* ctx, const wrach::SolveArgs& a, uint32_t count,
+                               cudaStream_t st, const float2** q, After after) {
+  const float2* src = a.tp_pos;
+  for (uint32_t it = 0; it < count; ++it) {
+    float2* dst = (it & 1) ? ctx->q2 : ctx->q1;
+    const cudaError_t e = wrach::launch_jacobi_iteration(a, src, dst, st);
+    if (e != cudaSuccess) return e;
+    after();
+    src = dst;
+  }
+  *q = src;
+  return cudaSuccess;
+}
 
 }  // namespace host
 }  // namespace wrach

@@ -13,15 +13,19 @@
 //   scan     exclusive scan of the per-cell counts, one block per tile of
 //            2048 cells; a tile's prefix is the sum of the earlier tiles'
 //            sums (already final, so no block waits); it writes the
-//            cell-start table, clears the counts and lists the cells of more
-//            than kSmallCell particles (the pass that takes the tickets
-//            empties that list first)
+//            cell-start table and (extended physics) the capped table of the
+//            taking-part particles from the counts capped at the cell
+//            capacity, clears the counts and lists the cells of more than
+//            kSmallCell particles (the pass that takes the tickets empties
+//            that list first)
 //   scatter  source index and cell of every particle to table start + ticket
 //            (arrival order inside a cell)
 //   place    the stable order: inside a cell, a particle's rank is the number
 //            of the cell's particles with a smaller source index; then the
-//            gather of positions, velocities and cells into that slot.  Cells
-//            of up to kSmallCell particles are ranked by one thread per slot
+//            gather of positions, velocities and cells into that slot, and of
+//            the taking-part particles' positions and cells into the
+//            compacted arrays.  Cells of up to kSmallCell particles are
+//            ranked by one thread per slot
 //   cells    one block per listed cell: up to kBigCell particles a bitonic
 //            sort of the source indices in shared memory, more than that a
 //            block-wide LSD radix sort of them in global memory; then the
@@ -51,7 +55,8 @@ __global__ void __launch_bounds__(256) k_cs_count(RebinArgs a) {
   for (uint32_t base = i - lane; base < a.n; base += stride) {
     const uint32_t j = base + lane;
     const uint32_t k = j < a.n ? a.keys[j] : a.ncells;
-    const uint32_t t = warp_ticket(k, a.ncells, a.counts, a.tile_sums, kCountScanShift);
+    const uint32_t t = warp_ticket(k, a.ncells, a.counts, a.tile_sums, kCountScanShift, a.tp_cap,
+                                   a.tp_cap ? a.tile_sums_cap : nullptr);
     if (j < a.n) a.ticket[j] = t;
   }
 }
@@ -73,6 +78,7 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red) {
 // block waits for another.
 __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
   __shared__ uint32_t warp_sum[kScanThreads / 32], red[kScanThreads / 32];
+  __shared__ uint32_t warp_cap[kScanThreads / 32];
   const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const uint32_t tile = blockIdx.x, n = a.ncells;
   if (tile == 0 && t == 0 && !a.force_general) a.ctrl->frames += 1;
@@ -89,29 +95,48 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
 #pragma unroll
     for (uint32_t u = 0; u < kScanPer; ++u) v[u] = c0 + u < n ? __ldcg(a.counts + c0 + u) : 0u;
   }
-  uint32_t sum = 0;
+  // the capped counts (the taking-part particles) when the capped table is wanted
+  const uint32_t cap = a.tp_cap;
+  uint32_t sum = 0, csum = 0;
 #pragma unroll
-  for (uint32_t u = 0; u < kScanPer; ++u) sum += v[u];
-  // the earlier tiles' total
-  uint32_t pre = 0;
-  for (uint32_t u = t; u < tile; u += kScanThreads) pre += __ldcg(a.tile_sums + u);
+  for (uint32_t u = 0; u < kScanPer; ++u) {
+    sum += v[u];
+    csum += min(v[u], cap);
+  }
+  // the earlier tiles' totals
+  uint32_t pre = 0, cpre = 0;
+  for (uint32_t u = t; u < tile; u += kScanThreads) {
+    pre += __ldcg(a.tile_sums + u);
+    if (cap) cpre += __ldcg(a.tile_sums_cap + u);
+  }
   const uint32_t prefix = block_sum(pre, red);
-  // block-wide exclusive scan of the per-thread sums
-  uint32_t x = sum;
+  const uint32_t cprefix = cap ? block_sum(cpre, red) : 0u;
+  // block-wide exclusive scans of the per-thread sums
+  uint32_t x = sum, cx = csum;
 #pragma unroll
   for (uint32_t o = 1; o < 32; o <<= 1) {
     const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
+    const uint32_t cy = __shfl_up_sync(0xffffffffu, cx, o);
+    if (lane >= o) {
+      x += y;
+      cx += cy;
+    }
   }
-  if (lane == 31) warp_sum[warp] = x;
+  if (lane == 31) {
+    warp_sum[warp] = x;
+    warp_cap[warp] = cx;
+  }
   __syncthreads();
-  uint32_t before = 0, total = 0;
+  uint32_t before = 0, total = 0, cbefore = 0, ctotal = 0;
 #pragma unroll
   for (uint32_t w = 0; w < kScanThreads / 32; ++w) {
     before += w < warp ? warp_sum[w] : 0u;
     total += warp_sum[w];
+    cbefore += w < warp ? warp_cap[w] : 0u;
+    ctotal += warp_cap[w];
   }
   uint32_t run = prefix + before + x - sum;
+  uint32_t crun = cprefix + cbefore + cx - csum;
   // the large cells' work list (at most n / (kSmallCell + 1) cells qualify,
   // and big_cap is larger)
 #pragma unroll
@@ -120,6 +145,28 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
       const uint32_t w = atomicAdd(&a.ctrl->big_count, 1u);
       if (w < a.big_cap) a.big_list[w] = c0 + u;
     }
+  }
+  if (cap) {
+    // the capped table (compacted starts of the cells' taking-part particles)
+    if (c0 + kScanPer <= n) {
+      uint4* dst = reinterpret_cast<uint4*>(a.ct_new + c0);
+#pragma unroll
+      for (uint32_t u = 0; u < kScanPer / 4; ++u) {
+        uint4 q;
+        q.x = crun; crun += min(v[4 * u], cap);
+        q.y = crun; crun += min(v[4 * u + 1], cap);
+        q.z = crun; crun += min(v[4 * u + 2], cap);
+        q.w = crun; crun += min(v[4 * u + 3], cap);
+        dst[u] = q;
+      }
+    } else {
+#pragma unroll
+      for (uint32_t u = 0; u < kScanPer; ++u) {
+        if (c0 + u < n) a.ct_new[c0 + u] = crun;
+        crun += min(v[u], cap);
+      }
+    }
+    if (t == 0 && (tile + 1) * kScanTile >= n) a.ct_new[n] = cprefix + ctotal;
   }
   if (c0 + kScanPer <= n) {
     uint4* dst = reinterpret_cast<uint4*>(a.cs_new + c0);
@@ -150,7 +197,10 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
 __global__ void __launch_bounds__(256) k_cs_scatter(RebinArgs a, uint32_t ntiles) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   // the scan has read the tile sums: clear them for the next rebin
-  for (uint32_t u = i; u < ntiles; u += gridDim.x * blockDim.x) a.tile_sums[u] = 0u;
+  for (uint32_t u = i; u < ntiles; u += gridDim.x * blockDim.x) {
+    a.tile_sums[u] = 0u;
+    if (a.tp_cap) a.tile_sums_cap[u] = 0u;
+  }
   if (i >= a.n) return;
   const uint32_t k = a.keys[i];
   if (k >= a.ncells) return;
@@ -161,12 +211,22 @@ __global__ void __launch_bounds__(256) k_cs_scatter(RebinArgs a, uint32_t ntiles
   }
 }
 
-__device__ __forceinline__ void place_one(const RebinArgs& a, uint32_t slot, uint32_t src,
-                                          uint32_t cell, uint32_t& overflow) {
+// The particle of source index `src` into `slot`, rank `rank` inside its
+// cell; a taking-part one (rank < tp_cap) also into the compacted arrays.
+__device__ __forceinline__ void place_one(const RebinArgs& a, uint32_t slot, uint32_t rank,
+                                          uint32_t src, uint32_t cell, uint32_t& overflow) {
   if (slot < a.dst_capacity && src < a.n) {
-    a.pos_dst[slot] = a.pos_src[src];
+    const float2 p = a.pos_src[src];
+    a.pos_dst[slot] = p;
     a.vel_dst[slot] = a.vel_src[src];
     a.cell_dst[slot] = cell;
+    if (rank < a.tp_cap) {
+      const uint32_t t = a.ct_new[cell] + rank;
+      if (t < a.dst_capacity) {  // always true unless the scan timed out
+        a.tp_pos[t] = p;
+        a.tp_cell[t] = cell;
+      }
+    }
   } else {
     ++overflow;
   }
@@ -191,7 +251,7 @@ __global__ void __launch_bounds__(256) k_cs_place(RebinArgs a) {
     const uint32_t me = a.idx_tmp[q];
     uint32_t rank = 0;
     for (uint32_t m = c0; m < s1; ++m) rank += a.idx_tmp[m] < me ? 1u : 0u;
-    place_one(a, c0 + rank, me, k, overflow);
+    place_one(a, c0 + rank, rank, me, k, overflow);
   }
   add_overflow(a, overflow);
 }
@@ -272,7 +332,7 @@ __global__ void __launch_bounds__(kBigThreads) k_cs_big(RebinArgs a) {
     const uint32_t s = s1 > s0 ? s1 - s0 : 0u;
     if (s > kBigCell) {
       const uint32_t* sorted = block_radix_sort(a.idx_tmp + s0, a.idx_alt + s0, s, key_bits);
-      for (uint32_t r = threadIdx.x; r < s; r += kBigThreads) place_one(a, s0 + r, sorted[r], k, overflow);
+      for (uint32_t r = threadIdx.x; r < s; r += kBigThreads) place_one(a, s0 + r, r, sorted[r], k, overflow);
       if (threadIdx.x == 0) atomicAdd(&a.ctrl->huge_cells, 1u);
       __syncthreads();
       continue;
@@ -296,7 +356,7 @@ __global__ void __launch_bounds__(kBigThreads) k_cs_big(RebinArgs a) {
         __syncthreads();
       }
     }
-    for (uint32_t r = threadIdx.x; r < s; r += kBigThreads) place_one(a, s0 + r, sv[r], k, overflow);
+    for (uint32_t r = threadIdx.x; r < s; r += kBigThreads) place_one(a, s0 + r, r, sv[r], k, overflow);
     __syncthreads();
   }
   add_overflow(a, overflow);

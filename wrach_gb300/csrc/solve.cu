@@ -4,8 +4,9 @@
 //
 // Reference-mode kernel: one thread per cell, the sequential sweep of
 // World::physics_for_cell (shaders/physics/src/cell.rs:52-95).
-// Extended-mode kernel: one thread per particle, a Jacobi iteration over the
-// particle's 3x3 cell neighbourhood.
+// Extended-mode kernels: one thread per taking-part particle (compacted), a
+// Jacobi iteration over the particle's 3x3 cell neighbourhood; the last
+// iteration one thread per particle.
 #include "wrach_internal.cuh"
 #include "wrach_kernels.h"
 
@@ -86,186 +87,189 @@ k_solve_reference(const WorldDev* __restrict__ worlds, int nworlds,
   publish_flags(ctrl, flags);
 }
 
-// Extended mode, one Jacobi iteration, one thread per particle.  As in the
+// Extended mode (3x3 cells, Jacobi iterations, gravity).  As in the
 // reference (cell.rs:29-30, 79-95) only the first `cap` particles of a cell
 // take part in the pushes, as pushed particles and as neighbours; the rest of
-// an over-full cell keep their position.  The neighbour order is fixed (3x3
-// cells in row-major order, table order inside a cell), so the sum is
-// deterministic.
+// an over-full cell keep their position.  The neighbour order is fixed (the
+// 3x3 cells in row-major order, table order inside a cell), so each
+// particle's push sum is deterministic.
 //
-// Two passes: pass 1 marks, per neighbour row, the candidates within reach
-// with an exact squared-distance test (cheap, every lane); pass 2 applies
-// the reference's push (IEEE square root and division) to those only, in
-// candidate order, in one loop over the three rows' marks.  A row whose
-// cells before the last are within capacity is one contiguous range of
-// candidates, scanned in one loop; other rows keep 16 mark bits per cell.
-//
-// FINAL fuses gravity, integration, boundaries, the velocity clamp and the
-// key emission.  METRICS (final pass only) also writes the block's sums for
-// the surrogate's fallback gate to part[blockIdx.x * 8 + k]: [0] sum and [1]
-// max over taking-part particles of the deepest overlap max(0, min_d -
-// distance) with a pushing neighbour (measured on the pass's input), [2] the
-// number of taking-part particles, [3] the kinetic energy of the output and
-// [4] the kinetic energy a plain frame gives (gravity, the clamp and wall
-// reflections only change the velocity).  A launch whose `run_if` flag reads
-// 0 returns at once.
-template <bool FINAL, bool METRICS>
+// The iterations run over the compacted taking-part particles (the capped
+// table ct of the rebin): there a neighbour row of the 3x3 search is one
+// contiguous range [ct[row + x0], ct[row + x1 + 1]) whatever the cells'
+// occupancy, and the particles that take no part cost nothing.  Per row, the
+// candidates within reach are marked with an exact squared-distance test
+// (cheap, every candidate), then the reference's push (IEEE square root and
+// division) is applied to the marked ones only, in candidate order, in one
+// loop over the three rows' marks, so that a lane moves on to its next row
+// without waiting for the warp's other lanes to finish the current one.
+
+__device__ __forceinline__ uint32_t low_bit(uint32_t m) { return __ffs((int)m) - 1; }
+__device__ __forceinline__ uint32_t low_bit(uint64_t m) { return __ffsll((long long)m) - 1; }
+
+// The push sum (ax, ay) of the compacted particle t of cell c at q_t = qi2,
+// over the compacted iterate q.  Mask holds one bit per candidate of a row:
+// 3 * cap bits.  METRICS: pen = the deepest overlap min_d - distance with a
+// pushing neighbour.
+template <typename Mask, bool METRICS>
+__device__ __forceinline__ void tp_push(const WorldDev& w, const PhysDev& ph,
+                                        const uint32_t* __restrict__ ct,
+                                        const f32x2* __restrict__ q, f32x2 qi2, uint32_t c,
+                                        uint32_t t, float& ax, float& ay, float& pen) {
+  uint32_t cx, cy;
+  cell_xy(w, c - w.cell_off, cx, cy);
+  const uint32_t x0 = cx > 0 ? cx - 1 : 0;
+  const uint32_t x1 = cx + 1 < w.gx ? cx + 1 : w.gx - 1;
+  // the rows' compacted ranges first: independent loads
+  uint32_t rs[3], re[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int ny = (int)cy - 1 + r;
+    const bool ok = ny >= 0 && ny < (int)w.gy;
+    const uint32_t rb = w.cell_off + (uint32_t)(ok ? ny : 0) * w.gx;
+    rs[r] = ok ? ct[rb + x0] : 0u;
+    re[r] = ok ? ct[rb + x1 + 1] : 0u;
+  }
+  // the candidates within reach, two per step (an odd last step tests its
+  // one candidate twice and keeps the first result); a NaN distance counts as
+  // within reach, as in the reference's test
+  Mask rmask[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    Mask close = 0;
+    const uint32_t s0 = rs[r], e = re[r];
+    for (uint32_t j = s0; j < e; j += 2) {
+      const uint32_t j1 = min(j + 1, e - 1);
+      const f32x2 da = f2_sub(q[j], qi2), db = f2_sub(q[j1], qi2);
+      const bool ca = !(f2_len2(da) >= ph.skip_d2);
+      const bool cb = j + 1 < e && !(f2_len2(db) >= ph.skip_d2);
+      close |= (Mask)((ca ? 1u : 0u) | (cb ? 2u : 0u)) << (j - s0);
+    }
+    // the particle itself (in the middle row) is not its own neighbour
+    if (r == 1) close &= ~((Mask)1 << (t - s0));
+    rmask[r] = close;
+  }
+  // the reference's push for those, in candidate order
+  Mask cur = rmask[0];
+  uint32_t base = rs[0];
+  Mask next1 = rmask[1], next2 = rmask[2];
+  for (;;) {
+    if (cur == 0) {
+      if (next1) {
+        cur = next1;
+        next1 = 0;
+        base = rs[1];
+      } else if (next2) {
+        cur = next2;
+        next2 = 0;
+        base = rs[2];
+      } else {
+        break;
+      }
+    }
+    const uint32_t b = low_bit(cur);
+    cur &= cur - 1;
+    const f32x2 dd = f2_sub(q[base + b], qi2);
+    float d;
+    const float f = push_factor_within(f2_x(dd), f2_y(dd), ph.min_d, d);
+    if (METRICS) pen = fmaxf(pen, __fsub_rn(ph.min_d, d));
+    // scalar: a paired multiply feeding a paired add may be fused
+    ax = __fadd_rn(ax, __fmul_rn(f2_x(dd), f));
+    ay = __fadd_rn(ay, __fmul_rn(f2_y(dd), f));
+  }
+}
+
+// One Jacobi iteration but the last, one thread per compacted (taking-part)
+// particle: q' = q - push sum.  The grid covers every particle of the frame;
+// threads past the compacted count ct[ncells] return.  A launch whose
+// `run_if` flag reads 0 returns at once.
+template <typename Mask>
 __global__ void __launch_bounds__(512)
-k_jacobi(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
-         uint32_t n, int do_push, const uint32_t* __restrict__ cell_start,
-         const uint32_t* __restrict__ cell_of, const float2* __restrict__ qin,
-         float2* __restrict__ qout, const float2* __restrict__ vin,
-         float2* __restrict__ vout, uint32_t* __restrict__ keys, Ctrl* ctrl,
-         const uint32_t* __restrict__ run_if, float* __restrict__ part, CountDev count) {
-  static_assert(FINAL || !METRICS, "metrics come from the final pass");
+k_jacobi_tp(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32_t ncells,
+            const uint32_t* __restrict__ ct, const uint32_t* __restrict__ tp_cell,
+            const float2* __restrict__ qin, float2* __restrict__ qout,
+            const uint32_t* __restrict__ run_if) {
+  if (run_if && *run_if == 0u) return;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= __ldg(ct + ncells)) return;
+  const f32x2* __restrict__ q = reinterpret_cast<const f32x2*>(qin);
+  const uint32_t c = tp_cell[t];
+  const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
+  const f32x2 qi2 = q[t];
+  float ax = 0.f, ay = 0.f, pen = 0.f;
+  tp_push<Mask, false>(w, ph, ct, q, qi2, c, t, ax, ay, pen);
+  qout[t] = make_float2(__fsub_rn(f2_x(qi2), ax), __fsub_rn(f2_y(qi2), ay));
+}
+
+// The last iteration, one thread per frame particle: the push (taking-part
+// particles, from the compacted iterate q), then gravity, integration,
+// boundaries, the velocity clamp and the key emission, and the rebin's
+// tickets.  METRICS also writes the block's sums for the surrogate's
+// fallback gate to part[blockIdx.x * 8 + k]: [0] sum and [1] max over
+// taking-part particles of the deepest overlap max(0, min_d - distance) with
+// a pushing neighbour (measured on the pass's input), [2] the number of
+// taking-part particles, [3] the kinetic energy of the output and [4] the
+// kinetic energy a plain frame gives (gravity, the clamp and wall
+// reflections only change the velocity).  A launch whose `run_if` flag
+// reads 0 returns at once.
+template <typename Mask, bool METRICS>
+__global__ void __launch_bounds__(512)
+k_jacobi_final(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32_t n,
+               int do_push, const uint32_t* __restrict__ cell_start,
+               const uint32_t* __restrict__ ct, const uint32_t* __restrict__ cell_of,
+               const float2* __restrict__ pin, const float2* __restrict__ qtp,
+               float2* __restrict__ pout, const float2* __restrict__ vin,
+               float2* __restrict__ vout, uint32_t* __restrict__ keys, Ctrl* ctrl,
+               const uint32_t* __restrict__ run_if, float* __restrict__ part, CountDev count) {
   if (run_if && *run_if == 0u) return;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   // taking the tickets: the rebin's scan lists its large cells afresh
-  if (FINAL && count.ticket && i == 0) ctrl->big_count = 0u;
+  if (count.ticket && i == 0) ctrl->big_count = 0u;
   const bool live = i < n;
   uint32_t flags = 0;
   float pen = 0.f, taking = 0.f, ke = 0.f, ke_plain = 0.f;
-  WorldDev w;
-  float2 qi = make_float2(0.f, 0.f);
-  // the push sum, and the positions as packed pairs
-  float ax = 0.0f, ay = 0.0f;
-  const f32x2* __restrict__ q64 = reinterpret_cast<const f32x2*>(qin);
-  f32x2 qi2 = 0ull;
-  uint32_t key = count.ncells;  // no cell, unless the final pass computes one
+  uint32_t key = count.ncells;  // no cell
   if (live) {
     const uint32_t c = cell_of[i];
-    w = worlds[world_of_cell(worlds, nworlds, c)];
-    uint32_t cx, cy;
-    cell_xy(w, c - w.cell_off, cx, cy);
-    qi2 = q64[i];
-    qi = make_float2(f2_x(qi2), f2_y(qi2));
-    if (do_push && i - cell_start[c] < ph.cap) {
+    const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
+    const uint32_t t = tp_index(cell_start, ct, c, i, ph.cap);
+    float qx, qy;
+    if (t != 0xFFFFFFFFu) {
       if (METRICS) taking = 1.f;
-      // the table entries of the three neighbour rows first: independent
-      // loads, so their latencies overlap
-      const uint32_t x0 = cx > 0 ? cx - 1 : 0;
-      const uint32_t x1 = cx + 1 < w.gx ? cx + 1 : w.gx - 1;
-      uint32_t st[3][4];
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        const int ny = (int)cy - 1 + r;
-        const bool row_ok = ny >= 0 && ny < (int)w.gy;
-        const uint32_t rb = w.cell_off + (uint32_t)(row_ok ? ny : 0) * w.gx + x0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          st[r][k] = (row_ok && x0 + k <= x1 + 1) ? cell_start[rb + k] : 0u;
-      }
-      const uint32_t ncol = x1 - x0 + 1;  // 2 or 3 cells per row
-      static_assert(kMaxCellCapacity <= 16, "16 mask bits per cell");
-      // per row: the close mask and the map from mask bit b to candidate
-      // index, base + b + (b >= 16 ? adj1 : 0) + (b >= 32 ? adj2 : 0)
-      uint64_t rmask[3];
-      uint32_t rbase[3], radj1[3], radj2[3];
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        // the row's taking-part candidates: up to three cells of at most
-        // `cap` particles each; a NaN distance counts as within reach, as in
-        // the reference's test
-        const uint32_t s0 = st[r][0], s1 = st[r][1], s2 = st[r][2], s3 = st[r][3];
-        const uint32_t e0 = min(s1, s0 + ph.cap);
-        const uint32_t e1 = min(s2, s1 + ph.cap);
-        const uint32_t e2 = ncol == 3 ? min(s3, s2 + ph.cap) : s2;
-        uint64_t close = 0;
-        const bool merged = e0 == s1 && (ncol == 2 || e1 == s2);
-        rbase[r] = s0;
-        radj1[r] = merged ? 0u : s1 - s0 - 16u;
-        radj2[r] = merged ? 0u : s2 - s1 - 16u;
-        if (merged) {
-          // no over-full cell before the last: one contiguous range, two
-          // candidates per step (an odd last step tests its one candidate
-          // twice and keeps the first result)
-          const uint32_t e = ncol == 3 ? e2 : e1;
-          for (uint32_t j = s0; j < e; j += 2) {
-            const uint32_t j1 = min(j + 1, e - 1);
-            const f32x2 da = f2_sub(q64[j], qi2), db = f2_sub(q64[j1], qi2);
-            const bool ca = !(f2_len2(da) >= ph.skip_d2);
-            const bool cb = j + 1 < e && !(f2_len2(db) >= ph.skip_d2);
-            close |= (uint64_t)((ca ? 1u : 0u) | (cb ? 2u : 0u)) << (j - s0);
-          }
-          // the particle itself (in the middle row) is not its own neighbour
-          if (r == 1 && i >= s0 && i < e) close &= ~(1ull << (i - s0));
-        } else {
-          uint32_t k = 0;
-          for (uint32_t j = s0; j < e0; ++j, ++k) {
-            if ((r != 1 || j != i) && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
-          }
-          k = 16;
-          for (uint32_t j = s1; j < e1; ++j, ++k) {
-            if ((r != 1 || j != i) && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
-          }
-          k = 32;
-          for (uint32_t j = s2; j < e2; ++j, ++k) {
-            if ((r != 1 || j != i) && !(f2_len2(f2_sub(q64[j], qi2)) >= ph.skip_d2)) close |= 1ull << k;
-          }
-        }
-        rmask[r] = close;
-      }
-      // pass 2: the reference's push for those, in candidate order
-      // (cell.rs:79-95).  One loop over the three rows' masks, so that a
-      // lane moves on to its next row without waiting for the warp's other
-      // lanes to finish the current one.
-      uint64_t cur = rmask[0];
-      uint32_t base = rbase[0], adj1 = radj1[0], adj2 = radj2[0];
-      uint64_t next1 = rmask[1], next2 = rmask[2];
-      for (;;) {
-        if (cur == 0) {
-          if (next1) {
-            cur = next1; next1 = 0;
-            base = rbase[1]; adj1 = radj1[1]; adj2 = radj2[1];
-          } else if (next2) {
-            cur = next2; next2 = 0;
-            base = rbase[2]; adj1 = radj1[2]; adj2 = radj2[2];
-          } else {
-            break;
-          }
-        }
-        const uint32_t b = __ffsll((long long)cur) - 1;
-        cur &= cur - 1;
-        const uint32_t j = base + b + (b >= 16 ? adj1 : 0u) + (b >= 32 ? adj2 : 0u);
-        const f32x2 dd = f2_sub(q64[j], qi2);
-        float d;
-        const float f = push_factor_within(f2_x(dd), f2_y(dd), ph.min_d, d);
-        if (METRICS) pen = fmaxf(pen, __fsub_rn(ph.min_d, d));
-        // scalar: a paired multiply feeding a paired add may be fused
-        ax = __fadd_rn(ax, __fmul_rn(f2_x(dd), f));
-        ay = __fadd_rn(ay, __fmul_rn(f2_y(dd), f));
-      }
-    }
-  }
-  if (live) {
-    const float qx = __fsub_rn(qi.x, ax), qy = __fsub_rn(qi.y, ay);
-    if (!FINAL) {
-      qout[i] = make_float2(qx, qy);
+      const f32x2* __restrict__ q = reinterpret_cast<const f32x2*>(qtp);
+      const f32x2 qi2 = q[t];
+      float ax = 0.f, ay = 0.f;
+      if (do_push) tp_push<Mask, METRICS>(w, ph, ct, q, qi2, c, t, ax, ay, pen);
+      qx = __fsub_rn(f2_x(qi2), ax);
+      qy = __fsub_rn(f2_y(qi2), ay);
     } else {
-      const float2 v = vin[i];
-      float ux = v.x, uy = __fsub_rn(v.y, ph.gravity);
-      float px = __fadd_rn(qx, ux), py = __fadd_rn(qy, uy);
-      enforce_limits(w, ph.vmax, px, py, ux, uy);
-      qout[i] = make_float2(px, py);
-      vout[i] = make_float2(ux, uy);
-      key = next_key(w, px, py, flags);
-      keys[i] = key;
-      if (METRICS) {
-        ke = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)));
-        const float cx = fminf(fmaxf(v.x, -ph.vmax), ph.vmax);
-        const float cy = fminf(fmaxf(__fsub_rn(v.y, ph.gravity), -ph.vmax), ph.vmax);
-        ke_plain = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
-      }
+      const float2 p = pin[i];
+      qx = p.x;
+      qy = p.y;
+    }
+    const float2 v = vin[i];
+    float ux = v.x, uy = __fsub_rn(v.y, ph.gravity);
+    float px = __fadd_rn(qx, ux), py = __fadd_rn(qy, uy);
+    enforce_limits(w, ph.vmax, px, py, ux, uy);
+    pout[i] = make_float2(px, py);
+    vout[i] = make_float2(ux, uy);
+    key = next_key(w, px, py, flags);
+    keys[i] = key;
+    if (METRICS) {
+      ke = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)));
+      const float cx = fminf(fmaxf(v.x, -ph.vmax), ph.vmax);
+      const float cy = fminf(fmaxf(__fsub_rn(v.y, ph.gravity), -ph.vmax), ph.vmax);
+      ke_plain = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
     }
   }
-  if (FINAL && count.ticket) {
+  if (count.ticket) {
     // the rebin's tickets (every lane of the warp takes part)
-    const uint32_t t = warp_ticket(key, count.ncells, count.counts, count.tile_sums,
-                                   count.tile_shift);
-    if (live) count.ticket[i] = t;
+    const uint32_t tk = warp_ticket(key, count.ncells, count.counts, count.tile_sums,
+                                    count.tile_shift, count.cap, count.tile_sums_cap);
+    if (live) count.ticket[i] = tk;
   }
-  if (FINAL) publish_flags(ctrl, flags);
+  publish_flags(ctrl, flags);
   if (METRICS) {
     // warp sums, then one thread sums the block's warps in a fixed order
     __shared__ float red[16][5];
@@ -304,24 +308,39 @@ cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_solve_extended(const SolveArgs& a, const float2* qin,
-                                  float2* qout, bool final_pass, int do_push,
-                                  cudaStream_t st) {
+cudaError_t launch_jacobi_iteration(const SolveArgs& a, const float2* qin, float2* qout,
+                                    cudaStream_t st) {
   if (a.n == 0) return cudaSuccess;
   const uint32_t threads = a.block ? a.block : 128;
   const uint32_t blocks = (a.n + threads - 1) / threads;
-  if (final_pass && a.part)
-    k_jacobi<true, true><<<blocks, threads, 0, st>>>(
-        a.worlds, a.nworlds, a.ph, a.n, do_push, a.cell_start, a.cell_of, qin,
-        qout, a.vel, a.vel_out, a.keys, a.ctrl, a.run_if, a.part, a.count);
-  else if (final_pass)
-    k_jacobi<true, false><<<blocks, threads, 0, st>>>(
-        a.worlds, a.nworlds, a.ph, a.n, do_push, a.cell_start, a.cell_of, qin,
-        qout, a.vel, a.vel_out, a.keys, a.ctrl, a.run_if, nullptr, a.count);
+  if (3 * a.ph.cap <= 32)
+    k_jacobi_tp<uint32_t><<<blocks, threads, 0, st>>>(a.worlds, a.nworlds, a.ph, a.ncells, a.ct,
+                                                       a.tp_cell, qin, qout, a.run_if);
   else
-    k_jacobi<false, false><<<blocks, threads, 0, st>>>(
-        a.worlds, a.nworlds, a.ph, a.n, do_push, a.cell_start, a.cell_of, qin,
-        qout, nullptr, nullptr, nullptr, a.ctrl, a.run_if, nullptr, CountDev{});
+    k_jacobi_tp<uint64_t><<<blocks, threads, 0, st>>>(a.worlds, a.nworlds, a.ph, a.ncells, a.ct,
+                                                       a.tp_cell, qin, qout, a.run_if);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_jacobi_final(const SolveArgs& a, const float2* qtp, int do_push,
+                                cudaStream_t st) {
+  if (a.n == 0) return cudaSuccess;
+  const uint32_t threads = a.block ? a.block : 128;
+  const uint32_t blocks = (a.n + threads - 1) / threads;
+  const bool narrow = 3 * a.ph.cap <= 32;
+#define WRACH_FINAL(MASK, METRICS, PART)                                                     \
+  k_jacobi_final<MASK, METRICS><<<blocks, threads, 0, st>>>(                                 \
+      a.worlds, a.nworlds, a.ph, a.n, do_push, a.cell_start, a.ct, a.cell_of, a.pos, qtp,    \
+      a.pos_out, a.vel, a.vel_out, a.keys, a.ctrl, a.run_if, PART, a.count)
+  if (a.part && narrow)
+    WRACH_FINAL(uint32_t, true, a.part);
+  else if (a.part)
+    WRACH_FINAL(uint64_t, true, a.part);
+  else if (narrow)
+    WRACH_FINAL(uint32_t, false, nullptr);
+  else
+    WRACH_FINAL(uint64_t, false, nullptr);
+#undef WRACH_FINAL
   return cudaGetLastError();
 }
 

@@ -675,8 +675,8 @@ k_knn_features(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uin
 // The surrogate correction of a frame in one pass: per tile of 256
 // particles, the features go to shared memory (padded rows, so the A-fragment
 // loads are conflict-free like the weights'), each warp runs the network on
-// 32 of the rows, and the correction is applied on the spot:
-// q = p + correction for taking-part particles, q = p otherwise.  `corr`
+// 32 of the rows, and the correction is applied on the spot: the compacted
+// iterate q_t = p + correction of each taking-part particle.  `corr`
 // (optional) receives the correction (zero for particles that do not take
 // part).  Persistent: the network is loaded once per block.
 constexpr uint32_t kFuseThreads = 256;
@@ -684,9 +684,9 @@ constexpr uint32_t kFuseThreads = 256;
 __global__ void __launch_bounds__(kFuseThreads, 3)
 k_surrogate_correct(MlpDev m, const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
                     uint32_t n, const uint32_t* __restrict__ cell_start,
-                    const uint32_t* __restrict__ cell_of, const float2* __restrict__ pos,
-                    const float2* __restrict__ vel, float2* __restrict__ q,
-                    float2* __restrict__ corr) {
+                    const uint32_t* __restrict__ ct, const uint32_t* __restrict__ cell_of,
+                    const float2* __restrict__ pos, const float2* __restrict__ vel,
+                    float2* __restrict__ q, float2* __restrict__ corr) {
   extern __shared__ __align__(16) uint8_t dyn[];
   SmemNet& s = *reinterpret_cast<SmemNet*>(dyn);
   uint32_t* sx = reinterpret_cast<uint32_t*>(dyn + sizeof(SmemNet));  // [256][kRow]
@@ -726,11 +726,15 @@ k_surrogate_correct(MlpDev m, const WorldDev* __restrict__ worlds, int nworlds, 
         for (uint32_t h = 0; h < 2; ++h) {
           const uint32_t r = r0 + g + 8 * h, idx = base + r;
           if (idx < n) {
-            const float2 p = pos[idx];
             const bool on = take[r] != 0u;
             const float cxv = on ? out[2 * h] : 0.f, cyv = on ? out[2 * h + 1] : 0.f;
             if (corr) corr[idx] = make_float2(cxv, cyv);
-            q[idx] = on ? make_float2(__fadd_rn(p.x, cxv), __fadd_rn(p.y, cyv)) : p;
+            if (on) {
+              // the compacted iterate of a taking-part particle
+              const float2 p = pos[idx];
+              const uint32_t tq = tp_index(cell_start, ct, cell_of[idx], idx, ph.cap);
+              q[tq] = make_float2(__fadd_rn(p.x, cxv), __fadd_rn(p.y, cyv));
+            }
           }
         }
       }
@@ -743,12 +747,20 @@ size_t correct_smem() {
   return sizeof(SmemNet) + (size_t)kFuseThreads * kRow * 4 + kFuseThreads * 4;
 }
 
-// target = q - p (the first K-1 iterations' correction)
-__global__ void k_target(uint32_t n, const float2* __restrict__ pos, const float2* __restrict__ q,
+// target = q - p, the first K-1 iterations' correction of frame particle i
+// (q compacted: zero for a particle that takes no part)
+__global__ void k_target(uint32_t n, PhysDev ph, const uint32_t* __restrict__ cell_start,
+                         const uint32_t* __restrict__ ct, const uint32_t* __restrict__ cell_of,
+                         const float2* __restrict__ pos, const float2* __restrict__ q,
                          float2* __restrict__ target) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float2 p = pos[i], v = q[i];
+  const uint32_t t = tp_index(cell_start, ct, cell_of[i], i, ph.cap);
+  if (t == 0xFFFFFFFFu) {
+    target[i] = make_float2(0.f, 0.f);
+    return;
+  }
+  const float2 p = pos[i], v = q[t];
   target[i] = make_float2(v.x - p.x, v.y - p.y);
 }
 
@@ -942,7 +954,7 @@ cudaError_t launch_surrogate_correct(const MlpDev& m, const SolveArgs& a, float2
   const int grid = sms * (per_sm > 0 ? per_sm : 1);
   const int need = (int)((a.n + kFuseThreads - 1) / kFuseThreads);
   k_surrogate_correct<<<need < grid ? need : grid, kFuseThreads, smem, st>>>(
-      m, a.worlds, a.nworlds, a.ph, a.n, a.cell_start, a.cell_of, a.pos, a.vel, q, corr);
+      m, a.worlds, a.nworlds, a.ph, a.n, a.cell_start, a.ct, a.cell_of, a.pos, a.vel, q, corr);
   return cudaGetLastError();
 }
 
@@ -983,10 +995,11 @@ cudaError_t launch_adam(const MlpDev& m, const float* grad, float* mom1, float* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_target(uint32_t n, const float2* pos, const float2* q, float2* target,
+cudaError_t launch_target(const SolveArgs& a, uint32_t n, const float2* q, float2* target,
                           cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_target<<<(n + 255) / 256, 256, 0, st>>>(n, pos, q, target);
+  k_target<<<(n + 255) / 256, 256, 0, st>>>(n, a.ph, a.cell_start, a.ct, a.cell_of, a.pos, q,
+                                            target);
   return cudaGetLastError();
 }
 

@@ -87,13 +87,9 @@ int enqueue_rebin(WrachContext* ctx) {
 int enqueue_plain_solve(WrachContext* ctx, const wrach::SolveArgs& a) {
   wrach::SolveArgs inner = a;
   inner.part = nullptr;
-  const float2* src = ctx->pos;
-  for (uint32_t it = 0; it + 1 < ctx->ph.iterations; ++it) {
-    float2* dst = (it & 1) ? ctx->q2 : ctx->q1;
-    CK(wrach::launch_solve_extended(inner, src, dst, false, 1, ctx->stream));
-    src = dst;
-  }
-  CK(wrach::launch_solve_extended(a, src, ctx->pos_o, true, 1, ctx->stream));
+  const float2* q = nullptr;
+  CK(enqueue_iterations(ctx, inner, ctx->ph.iterations - 1, ctx->stream, &q, []() {}));
+  CK(wrach::launch_jacobi_final(a, q, 1, ctx->stream));
   ctx->launches += ctx->ph.iterations;
   return WRACH_OK;
 }
@@ -243,13 +239,9 @@ int wrach_surrogate_collect(WrachContext* ctx, uint32_t* total) {
     wrach::SolveArgs a = solve_args(ctx);
     // features of the frame, then the correction of its first K-1 iterations
     CK(wrach::launch_knn_features(a, S.x, ctx->stream));
-    const float2* src = ctx->pos;
-    for (uint32_t it = 0; it + 1 < ctx->ph.iterations; ++it) {
-      float2* dst = (it & 1) ? ctx->q2 : ctx->q1;
-      CK(wrach::launch_solve_extended(a, src, dst, false, 1, ctx->stream));
-      src = dst;
-    }
-    CK(wrach::launch_target(take, ctx->pos, src, S.tt + S.nsamples, ctx->stream));
+    const float2* q = nullptr;
+    CK(enqueue_iterations(ctx, a, ctx->ph.iterations - 1, ctx->stream, &q, []() {}));
+    CK(wrach::launch_target(a, take, q, S.tt + S.nsamples, ctx->stream));
     CK(cudaMemcpyAsync(S.tx + (size_t)S.nsamples * wrach::kMlpIn, S.x, (size_t)take * wrach::kMlpIn * 2,
                        cudaMemcpyDeviceToDevice, ctx->stream));
     ctx->launches += ctx->ph.iterations + 1;
@@ -268,14 +260,10 @@ int wrach_surrogate_evaluate(WrachContext* ctx, float* mse_network, float* mse_z
   wrach::SolveArgs a = solve_args(ctx);
   CK(wrach::launch_knn_features(a, S.x, ctx->stream));
   CK(wrach::launch_mlp_forward(S.m, S.x, ctx->n, S.corr, S.blocks, ctx->stream));
-  const float2* src = ctx->pos;
-  for (uint32_t it = 0; it + 1 < ctx->ph.iterations; ++it) {
-    float2* dst = (it & 1) ? ctx->q2 : ctx->q1;
-    CK(wrach::launch_solve_extended(a, src, dst, false, 1, ctx->stream));
-    src = dst;
-  }
+  const float2* q = nullptr;
+  CK(enqueue_iterations(ctx, a, ctx->ph.iterations - 1, ctx->stream, &q, []() {}));
   // the target lands in pos_o (scratch between frames)
-  CK(wrach::launch_target(ctx->n, ctx->pos, src, ctx->pos_o, ctx->stream));
+  CK(wrach::launch_target(a, ctx->n, q, ctx->pos_o, ctx->stream));
   CK(cudaMemsetAsync(S.metrics, 0, 8 * 4, ctx->stream));
   CK(wrach::launch_errors(a, S.corr, ctx->pos_o, S.metrics, ctx->stream));
   float h[8];
@@ -366,7 +354,7 @@ int wrach_surrogate_step(WrachContext* ctx, uint32_t nsteps, float max_penetrati
     } else {
       // the surrogate correction, the last plain iteration, the gate
       CK(wrach::launch_surrogate_correct(S.m, a, ctx->q1, nullptr, S.blocks, ctx->stream));
-      CK(wrach::launch_solve_extended(a, ctx->q1, ctx->pos_o, true, 1, ctx->stream));
+      CK(wrach::launch_jacobi_final(a, ctx->q1, 1, ctx->stream));
       CK(wrach::launch_gate(S.part, nparts, S.gate, 0, ctx->stream));
       // the plain solve of the same frame, run only when the gate failed it
       a.run_if = &S.gate->fallback;

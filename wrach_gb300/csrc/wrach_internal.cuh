@@ -167,10 +167,14 @@ __device__ __forceinline__ float push_factor_within(float ex, float ey, float mi
 // cell).  All 32 lanes of the warp call it together.  Per warp, one atomic
 // per cell present gives each particle its slot inside the cell (arrival
 // order, lane order inside the warp), and one atomic per tile of
-// 2^tile_shift cells adds the tile's particle count.  Returns the slot, or
+// 2^tile_shift cells adds the tile's particle count.  With `tile_sums_cap`
+// set, the tickets below `cap` are also added to their tile's capped sum:
+// a cell's tickets are 0 .. count-1, so those number min(count, cap), the
+// particles of the cell that take part in the pushes.  Returns the slot, or
 // 0xFFFFFFFF for no cell.
 __device__ __forceinline__ uint32_t warp_ticket(uint32_t k, uint32_t ncells, uint32_t* counts,
-                                                uint32_t* tile_sums, uint32_t tile_shift) {
+                                                uint32_t* tile_sums, uint32_t tile_shift,
+                                                uint32_t cap, uint32_t* tile_sums_cap) {
   const uint32_t lane = threadIdx.x & 31;
   const bool valid = k < ncells;
   const uint32_t peers = __match_any_sync(0xffffffffu, valid ? k : 0xFFFFFFFFu);
@@ -178,27 +182,48 @@ __device__ __forceinline__ uint32_t warp_ticket(uint32_t k, uint32_t ncells, uin
   uint32_t first = 0;
   if (lane == leader && valid) first = atomicAdd(&counts[k], __popc(peers));
   first = __shfl_sync(0xffffffffu, first, leader);
+  const uint32_t ticket = valid ? first + __popc(peers & ((1u << lane) - 1u)) : 0xFFFFFFFFu;
   const uint32_t tile = valid ? k >> tile_shift : 0xFFFFFFFFu;
   const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+  const uint32_t cmask = tile_sums_cap ? __ballot_sync(0xffffffffu, valid && ticket < cap) : 0u;
   const uint32_t t0 = __shfl_sync(0xffffffffu, tile, vmask ? __ffs(vmask) - 1 : 0);
   if (__all_sync(0xffffffffu, !valid || tile == t0)) {
     // the common case: the warp's particles fall in one tile
     if (lane == 0 && vmask) atomicAdd(&tile_sums[t0], __popc(vmask));
+    if (lane == 0 && cmask) atomicAdd(&tile_sums_cap[t0], __popc(cmask));
   } else {
     const uint32_t tpeers = __match_any_sync(0xffffffffu, tile);
-    if (valid && lane == (uint32_t)(__ffs(tpeers) - 1)) atomicAdd(&tile_sums[tile], __popc(tpeers));
+    if (valid && lane == (uint32_t)(__ffs(tpeers) - 1)) {
+      atomicAdd(&tile_sums[tile], __popc(tpeers));
+      if (cmask & tpeers) atomicAdd(&tile_sums_cap[tile], __popc(cmask & tpeers));
+    }
   }
-  return valid ? first + __popc(peers & ((1u << lane) - 1u)) : 0xFFFFFFFFu;
+  return ticket;
 }
 
 // What the last Jacobi pass needs to take the counting sort's tickets.
 struct CountDev {
-  uint32_t* counts;     // ncells, zero on entry
-  uint32_t* tile_sums;  // one per tile of 2^tile_shift cells, zero on entry
-  uint32_t* ticket;     // n; nullptr: no tickets
+  uint32_t* counts;         // ncells, zero on entry
+  uint32_t* tile_sums;      // one per tile of 2^tile_shift cells, zero on entry
+  uint32_t* ticket;         // n; nullptr: no tickets
   uint32_t ncells;
   uint32_t tile_shift;
+  uint32_t cap;             // cell capacity of the taking-part particles
+  uint32_t* tile_sums_cap;  // per tile, tickets below cap (nullptr: not counted)
 };
+
+// The taking-part particles of a frame (the first `cap` of each cell, in
+// cell order) are also kept compacted: cell c's taking-part particles are
+// compacted entries [ct[c], ct[c + 1]) (the capped table, ct[ncells] = their
+// number), frame particle i of cell c takes part when i - cs[c] < cap, and
+// its compacted index is then ct[c] + i - cs[c].  Every neighbour row of the
+// 3x3 search is then one contiguous compacted range, over-full cells or not.
+__device__ __forceinline__ uint32_t tp_index(const uint32_t* __restrict__ cs,
+                                             const uint32_t* __restrict__ ct, uint32_t c,
+                                             uint32_t i, uint32_t cap) {
+  const uint32_t r = i - cs[c];
+  return r < cap ? ct[c] + r : 0xFFFFFFFFu;
+}
 
 // Packed pairs of binary32 values (x in the low word, as float2 in memory)
 // and sm_100-family paired arithmetic: each half rounds to nearest even on

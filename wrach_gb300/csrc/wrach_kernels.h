@@ -26,12 +26,24 @@ struct SolveArgs {
   const uint32_t* run_if;       // extended solve: skip the launch when *run_if == 0 (optional)
   float* part;                  // final extended pass: per-block metrics, 8 floats a block (optional)
   CountDev count;               // final extended pass: take the rebin's tickets (count.ticket set)
+  // the frame's taking-part particles, compacted (extended physics)
+  const uint32_t* ct;           // ncells + 1: capped table
+  const uint32_t* tp_cell;      // cell of each compacted particle
+  const float2* tp_pos;         // compacted positions of the binned state
 };
 
 cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st);
-cudaError_t launch_solve_extended(const SolveArgs& a, const float2* qin,
-                                  float2* qout, bool final_pass, int do_push,
-                                  cudaStream_t st);
+// One extended-mode iteration but the last, over the compacted taking-part
+// particles: qin and qout are compacted (the first iteration reads
+// a.tp_pos).
+cudaError_t launch_jacobi_iteration(const SolveArgs& a, const float2* qin, float2* qout,
+                                    cudaStream_t st);
+// The last iteration over every frame particle, from the compacted iterate
+// qtp (a.tp_pos when there is one iteration), into a.pos_out / a.vel_out /
+// a.keys (and the tickets and metrics when a.count / a.part are set);
+// do_push == 0 integrates only (no iterations).
+cudaError_t launch_jacobi_final(const SolveArgs& a, const float2* qtp, int do_push,
+                                cudaStream_t st);
 
 // Rebin: stable sort of `n` source particles by key into cell order, writing
 // a fresh cell-start table.  Persistent cooperative kernel.
@@ -66,6 +78,12 @@ struct RebinArgs {
   uint32_t* idx_alt;            // n: scratch of the in-memory sort of very large cells
   uint32_t* big_list;           // big_cap: cells of more than kSmallCell particles
   uint32_t big_cap;
+  // the taking-part particles, compacted (extended physics; tp_cap == 0: none)
+  uint32_t tp_cap;              // cell capacity: the first tp_cap of a cell take part
+  uint32_t* tile_sums_cap;      // per scan tile, its taking-part particles (zero between rebins)
+  uint32_t* ct_new;             // ncells + 1: capped table (compacted start of each cell)
+  float2* tp_pos;               // compacted positions
+  uint32_t* tp_cell;            // compacted cells
 };
 
 constexpr uint32_t kRebinThreads = 256;
@@ -163,8 +181,9 @@ struct GateState {
 };
 
 cudaError_t launch_knn_features(const SolveArgs& a, uint16_t* x, cudaStream_t st);
-// Fused surrogate correction of the binned frame: q = p + network(features)
-// for taking-part particles; `corr` optional.
+// Fused surrogate correction of the binned frame: the compacted iterate
+// q_t = p + network(features) of each taking-part particle; `corr` optional
+// (per frame particle).
 cudaError_t launch_surrogate_correct(const MlpDev& m, const SolveArgs& a, float2* q, float2* corr,
                                      int blocks, cudaStream_t st);
 cudaError_t launch_gate(const float* part, uint32_t nparts, GateState* gs, int mode,
@@ -181,7 +200,9 @@ cudaError_t launch_mlp_backward(const MlpDev& m, const uint16_t* x, const float2
                                 int blocks, cudaStream_t st);
 cudaError_t launch_adam(const MlpDev& m, const float* grad, float* mom1, float* mom2, float lr,
                         uint32_t step, cudaStream_t st);
-cudaError_t launch_target(uint32_t n, const float2* pos, const float2* q, float2* target,
+// target[i] = q_t - p_i for the first n frame particles, q compacted (zero
+// for a particle that takes no part).
+cudaError_t launch_target(const SolveArgs& a, uint32_t n, const float2* q, float2* target,
                           cudaStream_t st);
 cudaError_t launch_errors(const SolveArgs& a, const float2* corr, const float2* target, float* out,
                           cudaStream_t st);
