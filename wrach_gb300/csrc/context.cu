@@ -266,7 +266,7 @@ int enqueue_frame(WrachContext* ctx) {
     CK(enqueue_iterations(ctx, a, K > 0 ? K - 1 : 0, st, &q, [&]() { mark(ctx); }));
     CK(wrach::launch_jacobi_final(fin, q, K > 0 ? 1 : 0, st));
     mark(ctx);
-    ctx->launches += std::max<uint32_t>(K, 1);
+    ctx->launches += ctx->n ? std::max<uint32_t>(K, 1) : 0u;
   }
   const bool tickets_taken = ctx->ph.mode != WRACH_MODE_REFERENCE;
   wrach::RebinArgs r = rebin_args(ctx);
@@ -302,10 +302,19 @@ int enqueue_frame(WrachContext* ctx) {
   return WRACH_OK;
 }
 
-uint32_t frame_launches(const WrachContext* ctx) {
+// Steps wrach_profile_frame times in one frame: each solve launch, then
+// each rebin launch (an empty frame's extended solve launches nothing, but
+// still marks its steps).
+uint32_t frame_steps(const WrachContext* ctx) {
   const uint32_t rebin = wrach::count_sort_launches(ctx->n);
   if (ctx->ph.mode == WRACH_MODE_REFERENCE) return 1 + rebin;
   return std::max<uint32_t>(ctx->ph.iterations, 1) + rebin - (ctx->n ? 1 : 0);
+}
+
+// Kernel launches of one frame.
+uint32_t frame_launches(const WrachContext* ctx) {
+  if (ctx->ph.mode == WRACH_MODE_EXTENDED && !ctx->n) return wrach::count_sort_launches(0);
+  return frame_steps(ctx);
 }
 
 // One frame captured as a CUDA graph, instantiated once per table parity
@@ -784,7 +793,7 @@ int wrach_step(WrachContext* ctx, uint32_t nsteps) {
 int wrach_profile_frame(WrachContext* ctx, float* ms, uint32_t cap, uint32_t* count) {
   if (!ctx || !count) return WRACH_ERR_INVALID_ARGUMENT;
   DeviceGuard guard(ctx->device);
-  const uint32_t nl = frame_launches(ctx);
+  const uint32_t nl = frame_steps(ctx);
   *count = nl;
   if (!ms || cap < nl) return fail(ctx, WRACH_ERR_INVALID_ARGUMENT, "profile buffer too small");
   std::vector<cudaEvent_t> ev(nl + 1);

@@ -233,6 +233,15 @@ k_jacobi_final(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uin
   if (live) {
     const uint32_t c = cell_of[i];
     const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
+    // the velocity and, for the tickets' atomics, the counters of the
+    // particle's cell and of the cells above and below it (its next cell is
+    // almost always among their lines) are fetched before the push
+    const float2 v = vin[i];
+    if (count.ticket) {
+      prefetch_l2(count.counts + c);
+      prefetch_l2(count.counts + (c >= w.gx ? c - w.gx : c));
+      prefetch_l2(count.counts + min(c + w.gx, count.ncells - 1));
+    }
     const uint32_t t = tp_index(cell_start, ct, c, i, ph.cap);
     float qx, qy;
     if (t != 0xFFFFFFFFu) {
@@ -248,7 +257,6 @@ k_jacobi_final(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uin
       qx = p.x;
       qy = p.y;
     }
-    const float2 v = vin[i];
     float ux = v.x, uy = __fsub_rn(v.y, ph.gravity);
     float px = __fadd_rn(qx, ux), py = __fadd_rn(qy, uy);
     enforce_limits(w, ph.vmax, px, py, ux, uy);
