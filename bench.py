@@ -491,11 +491,14 @@ def run_surrogate(args):
     n = len(pos)
     sim = W.Simulation(W.WrachConfig(dimensions=dims, **cfg))
     sim.add_particles(pos, vel)
-    sim.surrogate_init(0, 24 * n)
+    # training rows from 2,000 plain frames of the trajectory: every 20th
+    # frame, every 4th taking-part particle of it (25 M rows)
+    train_frames, every, stride = 2000, 20, 4
+    sim.surrogate_init(0, (train_frames // every) * (n // stride + 1))
     t0 = time.perf_counter()
-    for f in range(480):
-        if f % 20 == 0:
-            sim.surrogate_collect()
+    for f in range(train_frames):
+        if f % every == 0:
+            rows = sim.surrogate_collect(stride)
         sim.step(1)
     sim.sync()
     collect_s = time.perf_counter() - t0
@@ -521,6 +524,18 @@ def run_surrogate(args):
     e1.record(fstream)
     torch.cuda.synchronize()
     fwd_s = e0.elapsed_time(e1) / 1000.0 / reps
+    # the fused surrogate pass alone (features from the 3x3 candidates, the
+    # network, the correction), on the same frame
+    corr = torch.zeros((n, 2), dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        sim.surrogate_correction(corr.data_ptr())
+    sim.sync()
+    e0.record(fstream)
+    for _ in range(reps):
+        sim.surrogate_correction(corr.data_ptr())
+    e1.record(fstream)
+    torch.cuda.synchronize()
+    fused_ms = e0.elapsed_time(e1) / reps
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             bf16_peak, peak_source = float(json.load(f)["bf16_tflops"]), "measured (burst)"
@@ -542,6 +557,13 @@ def run_surrogate(args):
         torch.cuda.synchronize()
         return ev[0].elapsed_time(ev[1]) / 1000.0, out
 
+    # the plain frame's launches, eager, on an early frame: a surrogate
+    # frame keeps the last iteration and the rebin, so with a free surrogate
+    # pass it would take the plain frame minus its first iterations
+    sim.set_particles(pos, vel)
+    sim.step(7)
+    prof = [float(x) for x in sim.profile_frame()]
+    iters = cfg["iterations"] - 1
     sim.set_particles(pos, vel)
     sim.step(3)                        # the plain frame graphs
     sim.surrogate_step(3, 0.2, 0.01)   # the fused kernel's set-up
@@ -563,6 +585,13 @@ def run_surrogate(args):
                           "reference_penetration_px": st["reference_penetration"],
                           "max_energy_drift": st["max_energy_drift"]},
             "speedup_vs_plain": plain_s / sur_s, "clocks": clocks.summary(),
+            "bound": {"plain_frame_launch_ms": prof,
+                      "replaced_iterations_ms": sum(prof[:iters]),
+                      "kept_ms": sum(prof[iters:]),
+                      "speedup_with_a_free_surrogate_pass": sum(prof) / sum(prof[iters:]),
+                      "fused_surrogate_pass_ms": fused_ms,
+                      "note": "eager launches of frame 8 (L2 warm); a surrogate frame keeps the last"
+                              " iteration and the rebin and adds two gate launches"},
             "network_roofline": {"bound": "tensor", "kernel": "k_mlp_forward (features precomputed)",
                                  "achieved": net_tflops, "peak": bf16_peak, "peak_source": peak_source,
                                  "unit": "TFLOP/s", "frac": net_tflops / bf16_peak,
@@ -574,7 +603,9 @@ def run_surrogate(args):
                             "plain_kinetic_energy": pen_plain[2],
                             "surrogate_kinetic_energy": pen_sur[2],
                             "kinetic_energy_ratio": pen_sur[2] / pen_plain[2] if pen_plain[2] else None},
-            "training": {"samples": 24 * n, "frames": 480, "steps": 4000, "batch": 16384,
+            "training": {"samples": rows, "frames": train_frames,
+                         "sampling": "every %dth frame, every %dth taking-part particle" % (every, stride),
+                         "steps": 4000, "batch": 16384,
                          "final_loss": loss, "collect_s": collect_s, "train_s": train_s,
                          "held_out_mse_ratio_vs_no_network": net / zero if zero else None}}
     sim.close()

@@ -266,8 +266,9 @@ const char *wrach_last_error(WrachContext *ctx);
 
 /* --- The learned solver surrogate (no counterpart in the reference) -------
  * A per-particle MLP (64 -> 64 -> 64 -> 2, GELU, BF16 weights on the tensor
- * cores, FP32 accumulation) reads each particle's 12 nearest neighbours'
- * relative positions and velocities plus its own velocity and predicts the
+ * cores, FP32 accumulation) reads the relative positions and velocities of
+ * each particle's 12 nearest neighbours in its 3x3 cells (the candidates of
+ * its Jacobi iterations) plus its own velocity and predicts the
  * position correction of the first iterations-1 Jacobi iterations of the
  * extended solve.  A surrogate frame applies that correction, runs the last
  * plain iteration (with integration, walls and clamp) and falls back to the
@@ -315,9 +316,11 @@ int wrach_surrogate_forward(WrachContext *ctx, const uint16_t *d_x,
 int wrach_surrogate_gradients(WrachContext *ctx, const uint16_t *d_x,
                               const float *d_t, uint32_t n, float *grad,
                               float *loss);
-/* Appends the current frame's features and plain-solver targets to the
- * training set (the frame does not advance); *total = rows collected. */
-int wrach_surrogate_collect(WrachContext *ctx, uint32_t *total);
+/* Appends features and plain-solver targets of the current frame's
+ * taking-part particles to the training set (the frame does not advance):
+ * every stride-th of them (0 = 1), from an offset that turns with each call;
+ * *total = rows collected.  Blocks. */
+int wrach_surrogate_collect(WrachContext *ctx, uint32_t stride, uint32_t *total);
 /* `steps` Adam steps on batches of `batch` collected rows; *loss = the last
  * batch's loss. */
 int wrach_surrogate_train(WrachContext *ctx, uint32_t steps, uint32_t batch,

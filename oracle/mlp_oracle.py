@@ -6,9 +6,10 @@ wrach_gb300/csrc/surrogate.cu:
 
   features   for each particle taking part in the solve (the first
              `capacity` of its cell), the 12 nearest taking-part particles in
-             the 5x5 cells around its cell by binary32 squared distance,
-             ties by index, each as (dx, dy, dvx, dvy) relative to the
-             particle; then its velocity; zero padding to 64; rounded to BF16.
+             the 3x3 cells around its cell (the candidates of its Jacobi
+             iterations) by binary32 squared distance, ties by index, each as
+             (dx, dy, dvx, dvy) relative to the particle; then its velocity;
+             zero padding to 64; rounded to BF16.
   network    64 -> 64 -> 64 -> 2, GELU (tanh form) after the hidden layers, BF16
              weights and activations, accumulation in float64 here (FP32 on
              the GPU).
@@ -135,8 +136,8 @@ def features(world_gx, world_gy, capacity, table, pos, vel):
         s, e = start[c], start[c + 1]
         cy, cx = divmod(c, world_gx)
         cand = []
-        for ny in range(max(cy - 2, 0), min(cy + 2, world_gy - 1) + 1):
-            for nx in range(max(cx - 2, 0), min(cx + 2, world_gx - 1) + 1):
+        for ny in range(max(cy - 1, 0), min(cy + 1, world_gy - 1) + 1):
+            for nx in range(max(cx - 1, 0), min(cx + 1, world_gx - 1) + 1):
                 nc = ny * world_gx + nx
                 js, je = start[nc], start[nc + 1]
                 cand.extend(range(js, min(je, js + capacity)))

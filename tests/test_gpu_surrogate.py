@@ -104,6 +104,24 @@ def test_training_beats_the_frame_without_the_network(W):
         assert np.mean(ratios) < 0.7
 
 
+def test_collect_takes_every_stride_th_taking_part_particle(W):
+    rng = np.random.default_rng(6)
+    dims = (50.0, 40.0)
+    pos = rng.uniform((0, 0), dims, size=(2500, 2)).astype(np.float32)
+    pos[:150] = (25.0 + rng.uniform(-1.0, 1.0, (150, 2))).astype(np.float32)  # over-full cells
+    vel = rng.normal(0, 0.7, size=pos.shape).astype(np.float32)
+    with _sim(W, dims, 4000) as sim:
+        sim.add_particles(pos, vel)
+        sim.surrogate_init(0, 100000)
+        p, v, table = sim.read_frame()
+        start = np.asarray(table, np.int64)[1:]
+        ntp = int(np.minimum(np.diff(start), 9).sum())
+        assert ntp < len(p)
+        # call 0: offset 0, stride 1; call 1: offset 1, stride 7
+        assert sim.surrogate_collect() == ntp
+        assert sim.surrogate_collect(stride=7) == ntp + (ntp - 1 + 6) // 7
+
+
 def test_fallback_gate(W):
     from wrach_gb300 import workloads
     dims, pos, vel = workloads.lattice(n=12000, width=200.0, height=120.0, sites=(139, 87))
@@ -191,3 +209,40 @@ def test_frame_metrics_match_numpy(W):
     assert abs(mean - pens.mean()) <= 1e-5 * max(pens.mean(), 1e-3)
     assert abs(mx - pens.max()) <= 1e-6
     assert abs(ke - 0.5 * (v.astype(np.float64) ** 2).sum()) <= 1e-5 * ke
+
+
+def test_surrogate_frames_hold_the_error_bounds(W):
+    """Trained on plain frames of a reduced lattice (60,000 particles at the
+    1M lattice's density), 320 gated surrogate frames (the configured gate:
+    fallback past 0.2 px of excess overlap or 1% of energy drift) stay within
+    the error bounds against 320 plain frames from the same state: averaged
+    over the last 160 frames (sampled every 32), the mean overlap at most
+    0.05 px above the plain frames' and the kinetic energy within 1%."""
+    from wrach_gb300 import workloads
+    dims, pos, vel = workloads.lattice(n=60000, width=480.0, height=272.0, sites=(334, 188))
+    with _sim(W, dims, 120000) as sur, _sim(W, dims, 120000) as plain:
+        sur.add_particles(pos, vel)
+        plain.add_particles(pos, vel)
+        sur.surrogate_init(0, 60000 * 64)
+        for f in range(320):
+            if f % 5 == 0:
+                sur.surrogate_collect()
+            sur.step(1)
+        sur.surrogate_train(1500, 8192, 2e-3)
+        sur.set_particles(pos, vel)
+        ms, mp, drift = [], [], 0.0
+        for chunk in range(10):
+            # chunks of 32 frames: one plain calibration frame and 31 gated
+            # surrogate frames each, as one continuous run would have them
+            st = sur.surrogate_step(32, max_penetration=0.2, max_energy_drift=0.01)
+            plain.step(32)
+            drift = max(drift, st["max_energy_drift"])
+            ms.append(sur.frame_metrics())
+            mp.append(plain.frame_metrics())
+    ms, mp = np.array(ms[5:]), np.array(mp[5:])
+    print("overlap %s vs %s px; kinetic energy %s vs %s; max drift %.4f"
+          % (np.round(ms[:, 0], 4), np.round(mp[:, 0], 4), np.round(ms[:, 2], 0),
+             np.round(mp[:, 2], 0), drift))
+    assert drift <= 0.01
+    assert ms[:, 0].mean() - mp[:, 0].mean() <= 0.05
+    assert abs(ms[:, 2].mean() / mp[:, 2].mean() - 1.0) <= 0.01

@@ -122,7 +122,7 @@ SIGNATURES = {
     "wrach_surrogate_features": (ctypes.c_int, [_P, _P, ctypes.c_uint32]),
     "wrach_surrogate_forward": (ctypes.c_int, [_P, _P, ctypes.c_uint32, _P]),
     "wrach_surrogate_gradients": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _F, _F]),
-    "wrach_surrogate_collect": (ctypes.c_int, [_P, _U]),
+    "wrach_surrogate_collect": (ctypes.c_int, [_P, ctypes.c_uint32, _U]),
     "wrach_surrogate_evaluate": (ctypes.c_int, [_P, _F, _F]),
     "wrach_frame_metrics": (ctypes.c_int, [_P, _F, _F, _F]),
     "wrach_surrogate_correction": (ctypes.c_int, [_P, _P]),

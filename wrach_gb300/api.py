@@ -254,9 +254,11 @@ class Simulation:
                                                       ctypes.byref(loss)))
         return g, float(loss.value)
 
-    def surrogate_collect(self):
+    def surrogate_collect(self, stride=1):
+        """Training rows from every stride-th taking-part particle of the
+        current frame; returns the rows collected so far."""
         total = ctypes.c_uint32(0)
-        self._check(self._L.wrach_surrogate_collect(self._ctx, ctypes.byref(total)))
+        self._check(self._L.wrach_surrogate_collect(self._ctx, int(stride), ctypes.byref(total)))
         return int(total.value)
 
     def surrogate_evaluate(self):

@@ -11,10 +11,11 @@
 //   q1, q2            extended-mode Jacobi iterates
 //   cell_of[2]        cell of each binned particle (u32)
 //   cs[2]             cell-start table, cells + 1 u32 (ping-pong per frame)
-//   ct[2], tp_pos[2], tp_cell[2]
+//   ct[2], tp_pos[2], tp_vel[2], tp_cell[2]
 //                     extended physics: the capped table (start of each
 //                     cell's taking-part particles among them all) and those
-//                     particles' positions and cells, compacted in cell order
+//                     particles' positions, velocities and cells, compacted in
+//                     cell order
 //   keys              next cell of each solve output (u32)
 //   kA kB iA iB       rebin scratch (tickets, slot cells, slot sources, sort ping-pong)
 //   tile_sums         rebin: particles per tile of 2048 cells (zero between frames)
@@ -87,6 +88,12 @@ void drop_graphs(WrachContext* ctx) {
       cudaGraphExecDestroy(g);
       g = nullptr;
     }
+  for (auto& row : ctx->sur.graph)
+    for (auto& g : row)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
 }
 
 void release(WrachContext* ctx) {
@@ -102,7 +109,7 @@ void release(WrachContext* ctx) {
                   ctx->cs[0], ctx->cs[1], ctx->keys, ctx->kA, ctx->kB,
                   ctx->iA, ctx->iB, ctx->tile_sums, ctx->ctrl, ctx->big_list,
                   ctx->ct[0], ctx->ct[1], ctx->tp_pos[0], ctx->tp_pos[1], ctx->tp_cell[0],
-                  ctx->tp_cell[1], ctx->tile_sums_cap,
+                  ctx->tp_cell[1], ctx->tile_sums_cap, ctx->tp_vel[0], ctx->tp_vel[1],
                   ctx->stage_pos, ctx->stage_vel, ctx->table_tmp, ctx->counts, ctx->render_cover, ctx->render_image,
                   ctx->gather_idx, ctx->gather_out, ctx->compact_sums};
   for (void* p : ptrs) dfree(p);
@@ -200,6 +207,8 @@ wrach::SolveArgs solve_args(WrachContext* ctx) {
   a.ct = ctx->ct[ctx->cur];
   a.tp_cell = ctx->tp_cell[ctx->cur];
   a.tp_pos = ctx->tp_pos[ctx->cur];
+  a.tp_vel = ctx->tp_vel[ctx->cur];
+  a.sms = ctx->sms;
   return a;
 }
 
@@ -234,6 +243,7 @@ wrach::RebinArgs rebin_args(WrachContext* ctx) {
     r.tile_sums_cap = ctx->tile_sums_cap;
     r.ct_new = ctx->ct[ctx->cur ^ 1];
     r.tp_pos = ctx->tp_pos[ctx->cur ^ 1];
+    r.tp_vel = ctx->tp_vel[ctx->cur ^ 1];
     r.tp_cell = ctx->tp_cell[ctx->cur ^ 1];
   }
   return r;
@@ -493,6 +503,7 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
       if ((e = dalloc(&ctx->ct[i], (size_t)ctx->ncells + 1)) != cudaSuccess) return oom(e);
       if ((e = cudaMemset(ctx->ct[i], 0, ((size_t)ctx->ncells + 1) * 4)) != cudaSuccess) return oom(e);
       if ((e = dalloc(&ctx->tp_pos[i], tc)) != cudaSuccess) return oom(e);
+      if ((e = dalloc(&ctx->tp_vel[i], tc)) != cudaSuccess) return oom(e);
       if ((e = dalloc(&ctx->tp_cell[i], tc)) != cudaSuccess) return oom(e);
     }
   }

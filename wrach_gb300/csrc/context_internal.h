@@ -54,6 +54,7 @@ struct WrachContext {
   // extended physics: the taking-part particles compacted (ping-pong with cs)
   uint32_t* ct[2] = {nullptr, nullptr};       // capped table, cells + 1
   float2* tp_pos[2] = {nullptr, nullptr};     // compacted positions
+  float2* tp_vel[2] = {nullptr, nullptr};     // compacted velocities
   uint32_t* tp_cell[2] = {nullptr, nullptr};  // compacted cells
   uint32_t* tile_sums_cap = nullptr;          // per scan tile, taking-part particles
   uint32_t ntiles = 0;
@@ -95,7 +96,13 @@ struct WrachContext {
     uint16_t* tx = nullptr;          // training features (max_samples rows)
     float2* tt = nullptr;            // training targets
     uint32_t nsamples = 0, max_samples = 0, step = 0;
+    uint32_t collects = 0;           // wrach_surrogate_collect calls since init
     int blocks = 0;
+    int correct_blocks = 0;          // grid of the fused correction kernel (one wave)
+    // surrogate frames as CUDA graphs: [table parity][calibration frame]
+    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    uint32_t graph_n[2][2] = {{0, 0}, {0, 0}};         // particle count at capture
+    uint32_t graph_launches[2][2] = {{0, 0}, {0, 0}};  // kernel launches per graph
   } sur;
 };
 

@@ -23,8 +23,8 @@
 //   place    the stable order: inside a cell, a particle's rank is the number
 //            of the cell's particles with a smaller source index; then the
 //            gather of positions, velocities and cells into that slot, and of
-//            the taking-part particles' positions and cells into the
-//            compacted arrays.  Cells of up to kSmallCell particles are
+//            the taking-part particles' positions, velocities and cells into
+//            the compacted arrays.  Cells of up to kSmallCell particles are
 //            ranked by one thread per slot
 //   cells    one block per listed cell: up to kBigCell particles a bitonic
 //            sort of the source indices in shared memory, more than that a
@@ -216,14 +216,15 @@ __global__ void __launch_bounds__(256) k_cs_scatter(RebinArgs a, uint32_t ntiles
 __device__ __forceinline__ void place_one(const RebinArgs& a, uint32_t slot, uint32_t rank,
                                           uint32_t src, uint32_t cell, uint32_t& overflow) {
   if (slot < a.dst_capacity && src < a.n) {
-    const float2 p = a.pos_src[src];
+    const float2 p = a.pos_src[src], v = a.vel_src[src];
     a.pos_dst[slot] = p;
-    a.vel_dst[slot] = a.vel_src[src];
+    a.vel_dst[slot] = v;
     a.cell_dst[slot] = cell;
     if (rank < a.tp_cap) {
       const uint32_t t = a.ct_new[cell] + rank;
       if (t < a.dst_capacity) {  // always true unless the scan timed out
         a.tp_pos[t] = p;
+        a.tp_vel[t] = v;
         a.tp_cell[t] = cell;
       }
     }

@@ -180,9 +180,10 @@ __device__ __forceinline__ void tp_push(const WorldDev& w, const PhysDev& ph,
 }
 
 // One Jacobi iteration but the last, one thread per compacted (taking-part)
-// particle: q' = q - push sum.  The grid covers every particle of the frame;
-// threads past the compacted count ct[ncells] return.  A launch whose
-// `run_if` flag reads 0 returns at once.
+// particle: q' = q - push sum, over the compacted count ct[ncells] (a
+// grid-stride loop; the plain frames' grid covers every particle of the
+// frame, so each thread takes one or none).  A launch whose `run_if` flag
+// reads 0 returns at once.
 template <typename Mask>
 __global__ void __launch_bounds__(512)
 k_jacobi_tp(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32_t ncells,
@@ -190,24 +191,26 @@ k_jacobi_tp(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32
             const float2* __restrict__ qin, float2* __restrict__ qout,
             const uint32_t* __restrict__ run_if) {
   if (run_if && *run_if == 0u) return;
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= __ldg(ct + ncells)) return;
+  const uint32_t ntp = __ldg(ct + ncells);
   const f32x2* __restrict__ q = reinterpret_cast<const f32x2*>(qin);
-  const uint32_t c = tp_cell[t];
-  const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
-  const f32x2 qi2 = q[t];
-  float ax = 0.f, ay = 0.f, pen = 0.f;
-  tp_push<Mask, false>(w, ph, ct, q, qi2, c, t, ax, ay, pen);
-  qout[t] = make_float2(__fsub_rn(f2_x(qi2), ax), __fsub_rn(f2_y(qi2), ay));
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntp; t += gridDim.x * blockDim.x) {
+    const uint32_t c = tp_cell[t];
+    const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
+    const f32x2 qi2 = q[t];
+    float ax = 0.f, ay = 0.f, pen = 0.f;
+    tp_push<Mask, false>(w, ph, ct, q, qi2, c, t, ax, ay, pen);
+    qout[t] = make_float2(__fsub_rn(f2_x(qi2), ax), __fsub_rn(f2_y(qi2), ay));
+  }
 }
 
-// The last iteration, one thread per frame particle: the push (taking-part
-// particles, from the compacted iterate q), then gravity, integration,
-// boundaries, the velocity clamp and the key emission, and the rebin's
-// tickets.  METRICS also writes the block's sums for the surrogate's
-// fallback gate to part[blockIdx.x * 8 + k]: [0] sum and [1] max over
-// taking-part particles of the deepest overlap max(0, min_d - distance) with
-// a pushing neighbour (measured on the pass's input), [2] the number of
+// The last iteration, one thread per frame particle (a grid-stride loop
+// over whole blocks of particles; the plain frames' grid covers them all):
+// the push (taking-part particles, from the compacted iterate q), then
+// gravity, integration, boundaries, the velocity clamp and the key emission,
+// and the rebin's tickets.  METRICS also writes the block's sums for the
+// surrogate's fallback gate to part[blockIdx.x * 8 + k]: [0] sum and [1] max
+// over taking-part particles of the deepest overlap max(0, min_d - distance)
+// with a pushing neighbour (measured on the pass's input), [2] the number of
 // taking-part particles, [3] the kinetic energy of the output and [4] the
 // kinetic energy a plain frame gives (gravity, the clamp and wall
 // reflections only change the velocity).  A launch whose `run_if` flag
@@ -223,59 +226,62 @@ k_jacobi_final(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uin
                const uint32_t* __restrict__ run_if, float* __restrict__ part, CountDev count) {
   if (run_if && *run_if == 0u) return;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   // taking the tickets: the rebin's scan lists its large cells afresh
-  if (count.ticket && i == 0) ctrl->big_count = 0u;
-  const bool live = i < n;
+  if (count.ticket && blockIdx.x == 0 && threadIdx.x == 0) ctrl->big_count = 0u;
   uint32_t flags = 0;
   float pen = 0.f, taking = 0.f, ke = 0.f, ke_plain = 0.f;
-  uint32_t key = count.ncells;  // no cell
-  if (live) {
-    const uint32_t c = cell_of[i];
-    const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
-    // the velocity and, for the tickets' atomics, the counters of the
-    // particle's cell and of the cells above and below it (its next cell is
-    // almost always among their lines) are fetched before the push
-    const float2 v = vin[i];
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const bool live = i < n;
+    uint32_t key = count.ncells;  // no cell
+    if (live) {
+      const uint32_t c = cell_of[i];
+      const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
+      // the velocity and, for the tickets' atomics, the counters of the
+      // particle's cell and of the cells above and below it (its next cell
+      // is almost always among their lines) are fetched before the push
+      const float2 v = vin[i];
+      if (count.ticket) {
+        prefetch_l2(count.counts + c);
+        prefetch_l2(count.counts + (c >= w.gx ? c - w.gx : c));
+        prefetch_l2(count.counts + min(c + w.gx, count.ncells - 1));
+      }
+      const uint32_t t = tp_index(cell_start, ct, c, i, ph.cap);
+      float qx, qy;
+      if (t != 0xFFFFFFFFu) {
+        if (METRICS) taking = __fadd_rn(taking, 1.f);
+        const f32x2* __restrict__ q = reinterpret_cast<const f32x2*>(qtp);
+        const f32x2 qi2 = q[t];
+        float ax = 0.f, ay = 0.f;
+        if (do_push) tp_push<Mask, METRICS>(w, ph, ct, q, qi2, c, t, ax, ay, pen);
+        qx = __fsub_rn(f2_x(qi2), ax);
+        qy = __fsub_rn(f2_y(qi2), ay);
+      } else {
+        const float2 p = pin[i];
+        qx = p.x;
+        qy = p.y;
+      }
+      float ux = v.x, uy = __fsub_rn(v.y, ph.gravity);
+      float px = __fadd_rn(qx, ux), py = __fadd_rn(qy, uy);
+      enforce_limits(w, ph.vmax, px, py, ux, uy);
+      pout[i] = make_float2(px, py);
+      vout[i] = make_float2(ux, uy);
+      key = next_key(w, px, py, flags);
+      keys[i] = key;
+      if (METRICS) {
+        ke = __fadd_rn(ke, __fmul_rn(0.5f, __fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy))));
+        const float cx = fminf(fmaxf(v.x, -ph.vmax), ph.vmax);
+        const float cy = fminf(fmaxf(__fsub_rn(v.y, ph.gravity), -ph.vmax), ph.vmax);
+        ke_plain = __fadd_rn(ke_plain,
+                             __fmul_rn(0.5f, __fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy))));
+      }
+    }
     if (count.ticket) {
-      prefetch_l2(count.counts + c);
-      prefetch_l2(count.counts + (c >= w.gx ? c - w.gx : c));
-      prefetch_l2(count.counts + min(c + w.gx, count.ncells - 1));
+      // the rebin's tickets (every lane of the warp takes part)
+      const uint32_t tk = warp_ticket(key, count.ncells, count.counts, count.tile_sums,
+                                      count.tile_shift, count.cap, count.tile_sums_cap);
+      if (live) count.ticket[i] = tk;
     }
-    const uint32_t t = tp_index(cell_start, ct, c, i, ph.cap);
-    float qx, qy;
-    if (t != 0xFFFFFFFFu) {
-      if (METRICS) taking = 1.f;
-      const f32x2* __restrict__ q = reinterpret_cast<const f32x2*>(qtp);
-      const f32x2 qi2 = q[t];
-      float ax = 0.f, ay = 0.f;
-      if (do_push) tp_push<Mask, METRICS>(w, ph, ct, q, qi2, c, t, ax, ay, pen);
-      qx = __fsub_rn(f2_x(qi2), ax);
-      qy = __fsub_rn(f2_y(qi2), ay);
-    } else {
-      const float2 p = pin[i];
-      qx = p.x;
-      qy = p.y;
-    }
-    float ux = v.x, uy = __fsub_rn(v.y, ph.gravity);
-    float px = __fadd_rn(qx, ux), py = __fadd_rn(qy, uy);
-    enforce_limits(w, ph.vmax, px, py, ux, uy);
-    pout[i] = make_float2(px, py);
-    vout[i] = make_float2(ux, uy);
-    key = next_key(w, px, py, flags);
-    keys[i] = key;
-    if (METRICS) {
-      ke = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)));
-      const float cx = fminf(fmaxf(v.x, -ph.vmax), ph.vmax);
-      const float cy = fminf(fmaxf(__fsub_rn(v.y, ph.gravity), -ph.vmax), ph.vmax);
-      ke_plain = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(cx, cx), __fmul_rn(cy, cy)));
-    }
-  }
-  if (count.ticket) {
-    // the rebin's tickets (every lane of the warp takes part)
-    const uint32_t tk = warp_ticket(key, count.ncells, count.counts, count.tile_sums,
-                                    count.tile_shift, count.cap, count.tile_sums_cap);
-    if (live) count.ticket[i] = tk;
   }
   publish_flags(ctrl, flags);
   if (METRICS) {
@@ -316,11 +322,20 @@ cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+uint32_t solve_blocks(const SolveArgs& a) {
+  const uint32_t threads = a.block ? a.block : 128;
+  const uint32_t blocks = (a.n + threads - 1) / threads;
+  // a launch that usually returns at once (the surrogate's fallback) strides
+  // over the frame with a few blocks per SM, so that skipping it is cheap
+  const uint32_t few = 4u * (uint32_t)(a.sms > 0 ? a.sms : 1) * (512u / threads);
+  return a.run_if && blocks > few ? few : blocks;
+}
+
 cudaError_t launch_jacobi_iteration(const SolveArgs& a, const float2* qin, float2* qout,
                                     cudaStream_t st) {
   if (a.n == 0) return cudaSuccess;
   const uint32_t threads = a.block ? a.block : 128;
-  const uint32_t blocks = (a.n + threads - 1) / threads;
+  const uint32_t blocks = solve_blocks(a);
   if (3 * a.ph.cap <= 32)
     k_jacobi_tp<uint32_t><<<blocks, threads, 0, st>>>(a.worlds, a.nworlds, a.ph, a.ncells, a.ct,
                                                        a.tp_cell, qin, qout, a.run_if);
@@ -334,7 +349,7 @@ cudaError_t launch_jacobi_final(const SolveArgs& a, const float2* qtp, int do_pu
                                 cudaStream_t st) {
   if (a.n == 0) return cudaSuccess;
   const uint32_t threads = a.block ? a.block : 128;
-  const uint32_t blocks = (a.n + threads - 1) / threads;
+  const uint32_t blocks = solve_blocks(a);
   const bool narrow = 3 * a.ph.cap <= 32;
 #define WRACH_FINAL(MASK, METRICS, PART)                                                     \
   k_jacobi_final<MASK, METRICS><<<blocks, threads, 0, st>>>(                                 \

@@ -2,9 +2,10 @@
 // position correction of the first K-1 Jacobi iterations of the extended
 // solve from the particle's k nearest neighbours.
 //
-//   features  k_knn_features: the 12 nearest taking-part particles within the
-//             5x5 cells around the particle (squared distance, ties by index),
-//             each as (dx, dy, dvx, dvy) relative to the particle, then the
+//   features  knn_row: the 12 nearest taking-part particles within the 3x3
+//             cells around the particle -- the candidates its Jacobi
+//             iterations scan (squared distance, ties by index) -- each as
+//             (dx, dy, dvx, dvy) relative to the particle, then the
 //             particle's own velocity; 50 values padded to 64, BF16.
 //   network   64 -> 64 -> 64 -> 2 (padded to 8), GELU (tanh form) after the
 //             two hidden layers; BF16 weights, FP32 accumulation, on the
@@ -563,29 +564,32 @@ __global__ void k_adam(MlpDev m, const float* __restrict__ grad, float* __restri
 
 constexpr uint32_t kK = kKnn;
 
-// Features of particle i into `row` (32 words, global or shared memory): the
-// 12 nearest taking-part particles (the first `cap` of each cell) in the 5x5
-// cells around the particle's cell, by binary32 squared distance (each
-// product and sum rounded on its own), ties by index; each as (dx, dy, dvx,
-// dvy) relative to the particle; then the own velocity; zero padding to 64.
-// A particle that does not take part (past the capacity of its cell) gets
-// all zeros.  Returns whether the particle takes part.
-__device__ __forceinline__ bool knn_row(const WorldDev* __restrict__ worlds, int nworlds,
-                                        const PhysDev& ph, const uint32_t* __restrict__ cell_start,
-                                        const uint32_t* __restrict__ cell_of,
-                                        const float2* __restrict__ pos,
-                                        const float2* __restrict__ vel, uint32_t i,
+// Features of the taking-part particle of compacted index t (cell c) into
+// `row` (32 words, global or shared memory): the 12 nearest taking-part
+// particles in the 3x3 cells around its cell -- the candidates of its Jacobi
+// iterations, one contiguous compacted range per neighbour row -- by binary32
+// squared distance (each product and sum rounded on its own), ties by index;
+// each as (dx, dy, dvx, dvy) relative to the particle; then the own
+// velocity; zero padding to 64.  Positions and velocities are the frame's
+// binned state, compacted (tpp, tpv).
+__device__ __forceinline__ void knn_row(const WorldDev& w, const uint32_t* __restrict__ ct,
+                                        const float2* __restrict__ tpp,
+                                        const float2* __restrict__ tpv, uint32_t c, uint32_t t,
                                         uint32_t* row) {
-  const uint32_t c = cell_of[i];
-  if (i - cell_start[c] >= ph.cap) {
-#pragma unroll
-    for (uint32_t k = 0; k < kIn / 2; ++k) row[k] = 0u;
-    return false;
-  }
-  const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
   uint32_t cx, cy;
   cell_xy(w, c - w.cell_off, cx, cy);
-  const float2 pi = pos[i], vi = vel[i];
+  const uint32_t x0 = cx > 0 ? cx - 1 : 0;
+  const uint32_t x1 = cx + 1 < w.gx ? cx + 1 : w.gx - 1;
+  uint32_t rs[3], re[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int ny = (int)cy - 1 + r;
+    const bool ok = ny >= 0 && ny < (int)w.gy;
+    const uint32_t rb = w.cell_off + (uint32_t)(ok ? ny : 0) * w.gx;
+    rs[r] = ok ? ct[rb + x0] : 0u;
+    re[r] = ok ? ct[rb + x1 + 1] : 0u;
+  }
+  const float2 pi = tpp[t], vi = tpv[t];
   float bd[kK];
   uint32_t bj[kK];
 #pragma unroll
@@ -593,59 +597,34 @@ __device__ __forceinline__ bool knn_row(const WorldDev* __restrict__ worlds, int
     bd[k] = INFINITY;
     bj[k] = 0xFFFFFFFFu;
   }
-  const int y0 = max((int)cy - 2, 0), y1 = min((int)cy + 2, (int)w.gy - 1);
-  const uint32_t x0 = cx >= 2 ? cx - 2 : 0, x1 = min(cx + 2, w.gx - 1);
-  const uint32_t ncol = x1 - x0 + 1;  // 3 to 5 cells per row
-  // one candidate: insert (distance, index), keeping the list ascending;
-  // every comparison against the old list first, then the shift
-  auto consider = [&](uint32_t j) {
-    const float2 pj = pos[j];
-    const float dx = __fsub_rn(pj.x, pi.x), dy = __fsub_rn(pj.y, pi.y);
-    const float d = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-    if (!(d < bd[kK - 1]) && !(d == bd[kK - 1] && j < bj[kK - 1])) return;
-    bool lt[kK];
+  // the candidates come in ascending index order (rows bottom-up, compacted
+  // order inside a row), so a tie in distance keeps the one already listed;
+  // each is inserted into the ascending list: every comparison against the
+  // old list first, then the shift
 #pragma unroll
-    for (uint32_t k = 0; k < kK; ++k) lt[k] = d < bd[k] || (d == bd[k] && j < bj[k]);
+  for (int r = 0; r < 3; ++r) {
+    for (uint32_t j = rs[r]; j < re[r]; ++j) {
+      if (j == t) continue;
+      const float2 pj = tpp[j];
+      const float dx = __fsub_rn(pj.x, pi.x), dy = __fsub_rn(pj.y, pi.y);
+      const float d = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+      if (!(d < bd[kK - 1])) continue;
+      bool lt[kK];
 #pragma unroll
-    for (uint32_t k = kK - 1; k > 0; --k) {
-      bd[k] = lt[k - 1] ? bd[k - 1] : (lt[k] ? d : bd[k]);
-      bj[k] = lt[k - 1] ? bj[k - 1] : (lt[k] ? j : bj[k]);
-    }
-    bd[0] = lt[0] ? d : bd[0];
-    bj[0] = lt[0] ? j : bj[0];
-  };
-  for (int ny = y0; ny <= y1; ++ny) {
-    // the row's table entries first: independent loads
-    const uint32_t rb = w.cell_off + (uint32_t)ny * w.gx + x0;
-    uint32_t st[6];
+      for (uint32_t k = 0; k < kK; ++k) lt[k] = d < bd[k];
 #pragma unroll
-    for (uint32_t k = 0; k < 6; ++k) st[k] = k <= ncol ? cell_start[rb + k] : 0u;
-    // a row whose cells before the last are within capacity is one
-    // contiguous range of candidates (the last cell clipped to capacity)
-    bool merged = true;
-#pragma unroll
-    for (uint32_t col = 0; col + 1 < 5; ++col)
-      if (col + 1 < ncol && st[col + 1] - st[col] > ph.cap) merged = false;
-    if (merged) {
-      const uint32_t last = ncol == 5 ? st[4] : (ncol == 4 ? st[3] : st[2]);
-      const uint32_t end = ncol == 5 ? st[5] : (ncol == 4 ? st[4] : st[3]);
-      const uint32_t e = min(end, last + ph.cap);
-      for (uint32_t j = st[0]; j < e; ++j)
-        if (j != i) consider(j);
-      continue;
-    }
-#pragma unroll
-    for (uint32_t col = 0; col < 5; ++col) {
-      if (col >= ncol) break;
-      const uint32_t js = st[col], je = min(st[col + 1], js + ph.cap);
-      for (uint32_t j = js; j < je; ++j)
-        if (j != i) consider(j);
+      for (uint32_t k = kK - 1; k > 0; --k) {
+        bd[k] = lt[k - 1] ? bd[k - 1] : (lt[k] ? d : bd[k]);
+        bj[k] = lt[k - 1] ? bj[k - 1] : (lt[k] ? j : bj[k]);
+      }
+      bd[0] = lt[0] ? d : bd[0];
+      bj[0] = lt[0] ? j : bj[0];
     }
   }
 #pragma unroll
   for (uint32_t k = 0; k < kK; ++k) {
     if (bj[k] != 0xFFFFFFFFu) {
-      const float2 pj = pos[bj[k]], vj = vel[bj[k]];
+      const float2 pj = tpp[bj[k]], vj = tpv[bj[k]];
       row[2 * k] = pack_bf16(__fsub_rn(pj.x, pi.x), __fsub_rn(pj.y, pi.y));
       row[2 * k + 1] = pack_bf16(__fsub_rn(vj.x, vi.x), __fsub_rn(vj.y, vi.y));
     } else {
@@ -656,55 +635,85 @@ __device__ __forceinline__ bool knn_row(const WorldDev* __restrict__ worlds, int
   row[2 * kK] = pack_bf16(vi.x, vi.y);
 #pragma unroll
   for (uint32_t k = 2 * kK + 1; k < kIn / 2; ++k) row[k] = 0u;
-  return true;
 }
 
-// Features of the binned state into x (BF16 [n][64]), one thread per
-// particle.
+__device__ __forceinline__ void zero_row(uint32_t* row) {
+#pragma unroll
+  for (uint32_t k = 0; k < kIn / 2; ++k) row[k] = 0u;
+}
+
+// Features of the binned frame into x (BF16 [n][64]), one thread per frame
+// particle; a particle that does not take part (past the capacity of its
+// cell) gets all zeros.
 __global__ void __launch_bounds__(256)
 k_knn_features(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32_t n,
-               const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ cell_of,
-               const float2* __restrict__ pos, const float2* __restrict__ vel,
-               uint16_t* __restrict__ x) {
+               const uint32_t* __restrict__ cell_start, const uint32_t* __restrict__ ct,
+               const uint32_t* __restrict__ cell_of, const float2* __restrict__ tpp,
+               const float2* __restrict__ tpv, uint16_t* __restrict__ x) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  knn_row(worlds, nworlds, ph, cell_start, cell_of, pos, vel, i,
-          reinterpret_cast<uint32_t*>(x + (size_t)i * kIn));
+  uint32_t* row = reinterpret_cast<uint32_t*>(x + (size_t)i * kIn);
+  const uint32_t c = cell_of[i];
+  const uint32_t t = tp_index(cell_start, ct, c, i, ph.cap);
+  if (t == 0xFFFFFFFFu) {
+    zero_row(row);
+    return;
+  }
+  knn_row(worlds[world_of_cell(worlds, nworlds, c)], ct, tpp, tpv, c, t, row);
 }
 
-// The surrogate correction of a frame in one pass: per tile of 256
-// particles, the features go to shared memory (padded rows, so the A-fragment
-// loads are conflict-free like the weights'), each warp runs the network on
-// 32 of the rows, and the correction is applied on the spot: the compacted
-// iterate q_t = p + correction of each taking-part particle.  `corr`
-// (optional) receives the correction (zero for particles that do not take
-// part).  Persistent: the network is loaded once per block.
+// Training samples of the binned frame: the features of the taking-part
+// particles t = phase + k * stride, k = 0, 1, ..., into rows k of x (at most
+// `rows`), and their targets q_t - p_t from the compacted iterate q (the
+// plain solver's first iterations) into target.
+__global__ void __launch_bounds__(256)
+k_samples(const WorldDev* __restrict__ worlds, int nworlds, uint32_t ncells,
+          const uint32_t* __restrict__ ct, const uint32_t* __restrict__ tp_cell,
+          const float2* __restrict__ tpp, const float2* __restrict__ tpv,
+          const float2* __restrict__ q, uint32_t stride, uint32_t phase, uint32_t rows,
+          uint16_t* __restrict__ x, float2* __restrict__ target) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t t = phase + k * stride;
+  if (k >= rows || t >= __ldg(ct + ncells)) return;
+  const uint32_t c = tp_cell[t];
+  knn_row(worlds[world_of_cell(worlds, nworlds, c)], ct, tpp, tpv, c, t,
+          reinterpret_cast<uint32_t*>(x + (size_t)k * kIn));
+  const float2 p = tpp[t], v = q[t];
+  target[k] = make_float2(v.x - p.x, v.y - p.y);
+}
+
+// The surrogate correction of a frame in one pass over its taking-part
+// particles (compacted): per tile of 256 of them, the features go to shared
+// memory (padded rows, so the A-fragment loads are conflict-free like the
+// weights'), each warp runs the network on 32 of the rows, and the
+// correction is applied on the spot: the compacted iterate q_t = p_t +
+// correction.  `corr` (optional) receives the correction at the frame index
+// of each taking-part particle.  Persistent: the network is loaded once per
+// block.
 constexpr uint32_t kFuseThreads = 256;
 
 __global__ void __launch_bounds__(kFuseThreads, 3)
-k_surrogate_correct(MlpDev m, const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph,
-                    uint32_t n, const uint32_t* __restrict__ cell_start,
-                    const uint32_t* __restrict__ ct, const uint32_t* __restrict__ cell_of,
-                    const float2* __restrict__ pos, const float2* __restrict__ vel,
+k_surrogate_correct(MlpDev m, const WorldDev* __restrict__ worlds, int nworlds,
+                    uint32_t ncells, const uint32_t* __restrict__ cell_start,
+                    const uint32_t* __restrict__ ct, const uint32_t* __restrict__ tp_cell,
+                    const float2* __restrict__ tpp, const float2* __restrict__ tpv,
                     float2* __restrict__ q, float2* __restrict__ corr) {
   extern __shared__ __align__(16) uint8_t dyn[];
   SmemNet& s = *reinterpret_cast<SmemNet*>(dyn);
   uint32_t* sx = reinterpret_cast<uint32_t*>(dyn + sizeof(SmemNet));  // [256][kRow]
-  uint32_t* take = sx + kFuseThreads * kRow;                          // [256]
   load_net(m, s, nullptr);
+  const uint32_t ntp = __ldg(ct + ncells);
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t g = lane >> 2, t = lane & 3;
-  for (uint32_t base = blockIdx.x * kFuseThreads; base < n; base += gridDim.x * kFuseThreads) {
-    const uint32_t i = base + threadIdx.x;
+  const uint32_t g = lane >> 2, t4 = lane & 3;
+  for (uint32_t base = blockIdx.x * kFuseThreads; base < ntp; base += gridDim.x * kFuseThreads) {
+    const uint32_t t = base + threadIdx.x;
     uint32_t* row = sx + threadIdx.x * kRow;
-    bool tk = false;
-    if (i < n) {
-      tk = knn_row(worlds, nworlds, ph, cell_start, cell_of, pos, vel, i, row);
+    if (t < ntp) {
+      const uint32_t c = tp_cell[t];
+      knn_row(worlds[world_of_cell(worlds, nworlds, c)], ct, tpp, tpv, c, t, row);
     } else {
-#pragma unroll
-      for (uint32_t k = 0; k < kIn / 2; ++k) row[k] = 0u;
+      zero_row(row);
     }
-    take[threadIdx.x] = tk;
     __syncthreads();
 #pragma unroll 1
     for (uint32_t rt = 0; rt < 2; ++rt) {
@@ -715,25 +724,23 @@ k_surrogate_correct(MlpDev m, const WorldDev* __restrict__ worlds, int nworlds, 
       const uint32_t* p1 = sx + (r0 + g + 8) * kRow;
 #pragma unroll
       for (uint32_t kk = 0; kk < 4; ++kk) {
-        ax[kk][0] = p0[kk * 8 + t];
-        ax[kk][1] = p1[kk * 8 + t];
-        ax[kk][2] = p0[kk * 8 + 4 + t];
-        ax[kk][3] = p1[kk * 8 + 4 + t];
+        ax[kk][0] = p0[kk * 8 + t4];
+        ax[kk][1] = p1[kk * 8 + t4];
+        ax[kk][2] = p0[kk * 8 + 4 + t4];
+        ax[kk][3] = p1[kk * 8 + 4 + t4];
       }
       mlp_tile_infer(s, lane, ax, out);
-      if (t == 0) {
+      if (t4 == 0) {
 #pragma unroll
         for (uint32_t h = 0; h < 2; ++h) {
-          const uint32_t r = r0 + g + 8 * h, idx = base + r;
-          if (idx < n) {
-            const bool on = take[r] != 0u;
-            const float cxv = on ? out[2 * h] : 0.f, cyv = on ? out[2 * h + 1] : 0.f;
-            if (corr) corr[idx] = make_float2(cxv, cyv);
-            if (on) {
-              // the compacted iterate of a taking-part particle
-              const float2 p = pos[idx];
-              const uint32_t tq = tp_index(cell_start, ct, cell_of[idx], idx, ph.cap);
-              q[tq] = make_float2(__fadd_rn(p.x, cxv), __fadd_rn(p.y, cyv));
+          const uint32_t idx = base + r0 + g + 8 * h;
+          if (idx < ntp) {
+            const float cxv = out[2 * h], cyv = out[2 * h + 1];
+            const float2 p = tpp[idx];
+            q[idx] = make_float2(__fadd_rn(p.x, cxv), __fadd_rn(p.y, cyv));
+            if (corr) {
+              const uint32_t c = tp_cell[idx];
+              corr[cell_start[c] + (idx - ct[c])] = make_float2(cxv, cyv);
             }
           }
         }
@@ -743,9 +750,7 @@ k_surrogate_correct(MlpDev m, const WorldDev* __restrict__ worlds, int nworlds, 
   }
 }
 
-size_t correct_smem() {
-  return sizeof(SmemNet) + (size_t)kFuseThreads * kRow * 4 + kFuseThreads * 4;
-}
+size_t correct_smem() { return sizeof(SmemNet) + (size_t)kFuseThreads * kRow * 4; }
 
 // target = q - p, the first K-1 iterations' correction of frame particle i
 // (q compacted: zero for a particle that takes no part)
@@ -931,30 +936,41 @@ cudaError_t launch_errors(const SolveArgs& a, const float2* corr, const float2* 
 
 cudaError_t launch_knn_features(const SolveArgs& a, uint16_t* x, cudaStream_t st) {
   if (a.n == 0) return cudaSuccess;
-  k_knn_features<<<(a.n + 255) / 256, 256, 0, st>>>(a.worlds, a.nworlds, a.ph, a.n,
-                                                    a.cell_start, a.cell_of, a.pos, a.vel, x);
+  k_knn_features<<<(a.n + 255) / 256, 256, 0, st>>>(a.worlds, a.nworlds, a.ph, a.n, a.cell_start,
+                                                    a.ct, a.cell_of, a.tp_pos, a.tp_vel, x);
   return cudaGetLastError();
+}
+
+cudaError_t launch_samples(const SolveArgs& a, const float2* q, uint32_t stride, uint32_t phase,
+                           uint32_t rows, uint16_t* x, float2* target, cudaStream_t st) {
+  if (rows == 0) return cudaSuccess;
+  k_samples<<<(rows + 255) / 256, 256, 0, st>>>(a.worlds, a.nworlds, a.ncells, a.ct, a.tp_cell,
+                                                a.tp_pos, a.tp_vel, q, stride, phase, rows, x,
+                                                target);
+  return cudaGetLastError();
+}
+
+int surrogate_correct_blocks(int device) {
+  const size_t smem = correct_smem();
+  if (cudaFuncSetAttribute(k_surrogate_correct, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return 0;
+  // persistent: one wave of co-resident blocks
+  int sms = 0, per_sm = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_surrogate_correct, kFuseThreads,
+                                                    smem) != cudaSuccess)
+    return 0;
+  return sms * (per_sm > 0 ? per_sm : 1);
 }
 
 cudaError_t launch_surrogate_correct(const MlpDev& m, const SolveArgs& a, float2* q, float2* corr,
                                      int blocks, cudaStream_t st) {
-  (void)blocks;
   if (a.n == 0) return cudaSuccess;
-  const size_t smem = correct_smem();
-  cudaError_t e = cudaFuncSetAttribute(k_surrogate_correct,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  // persistent: one wave of co-resident blocks
-  int dev = 0, sms = 0, per_sm = 0;
-  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_surrogate_correct, kFuseThreads,
-                                                         smem)) != cudaSuccess)
-    return e;
-  const int grid = sms * (per_sm > 0 ? per_sm : 1);
   const int need = (int)((a.n + kFuseThreads - 1) / kFuseThreads);
-  k_surrogate_correct<<<need < grid ? need : grid, kFuseThreads, smem, st>>>(
-      m, a.worlds, a.nworlds, a.ph, a.n, a.cell_start, a.ct, a.cell_of, a.pos, a.vel, q, corr);
+  k_surrogate_correct<<<need < blocks ? need : blocks, kFuseThreads, correct_smem(), st>>>(
+      m, a.worlds, a.nworlds, a.ncells, a.cell_start, a.ct, a.tp_cell, a.tp_pos, a.tp_vel, q,
+      corr);
   return cudaGetLastError();
 }
 

@@ -90,13 +90,41 @@ int enqueue_plain_solve(WrachContext* ctx, const wrach::SolveArgs& a) {
   const float2* q = nullptr;
   CK(enqueue_iterations(ctx, inner, ctx->ph.iterations - 1, ctx->stream, &q, []() {}));
   CK(wrach::launch_jacobi_final(a, q, 1, ctx->stream));
-  ctx->launches += ctx->ph.iterations;
+  ctx->launches += ctx->n ? ctx->ph.iterations : 0u;
   return WRACH_OK;
 }
 
 // every kCalibrationPeriod-th surrogate frame, the first included, is a
 // plain frame whose metrics become the gate's reference
 constexpr uint32_t kCalibrationPeriod = 32;
+
+// One surrogate frame, or a plain calibration frame, with no host
+// synchronisation: the gate decides on the device.
+int enqueue_surrogate_frame(WrachContext* ctx, int calibration) {
+  auto& S = ctx->sur;
+  wrach::SolveArgs a = solve_args(ctx);
+  a.part = S.part;
+  int rc;
+  if (calibration) {
+    // a plain frame: its metrics are the reference of the next frames
+    if ((rc = enqueue_plain_solve(ctx, a))) return rc;
+    CK(wrach::launch_gate(S.part, wrach::solve_blocks(a), S.gate, 2, ctx->stream));
+    ctx->launches += 1;
+  } else {
+    // the surrogate correction, the last plain iteration, the gate
+    CK(wrach::launch_surrogate_correct(S.m, a, ctx->q1, nullptr, S.correct_blocks, ctx->stream));
+    CK(wrach::launch_jacobi_final(a, ctx->q1, 1, ctx->stream));
+    CK(wrach::launch_gate(S.part, wrach::solve_blocks(a), S.gate, 0, ctx->stream));
+    // the plain solve of the same frame, run only when the gate failed it
+    // (its launches stride over the frame with few blocks, so skipping them
+    // is cheap), and the gate again on its metrics
+    a.run_if = &S.gate->fallback;
+    if ((rc = enqueue_plain_solve(ctx, a))) return rc;
+    CK(wrach::launch_gate(S.part, wrach::solve_blocks(a), S.gate, 1, ctx->stream));
+    ctx->launches += (ctx->n ? 2 : 0) + 2;
+  }
+  return enqueue_rebin(ctx);
+}
 
 }  // namespace
 
@@ -136,6 +164,8 @@ int wrach_surrogate_init(WrachContext* ctx, uint32_t seed, uint32_t max_samples)
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     S.blocks = sms > 0 ? 4 * sms : 64;
+    S.correct_blocks = wrach::surrogate_correct_blocks(ctx->device);
+    if (S.correct_blocks <= 0) return fail(ctx, WRACH_ERR_CUDA, "surrogate kernel set-up failed");
   }
   if (max_samples > S.max_samples) {
     dfree(S.tx);
@@ -148,6 +178,7 @@ int wrach_surrogate_init(WrachContext* ctx, uint32_t seed, uint32_t max_samples)
   }
   S.nsamples = 0;
   S.step = 0;
+  S.collects = 0;
   // Glorot-uniform weights from a fixed-seed generator, zero biases, a
   // small last layer so that the initial correction is near zero
   std::vector<float> p(kMlpParams, 0.0f);
@@ -229,22 +260,30 @@ int wrach_surrogate_gradients(WrachContext* ctx, const uint16_t* d_x, const floa
   return WRACH_OK;
 }
 
-int wrach_surrogate_collect(WrachContext* ctx, uint32_t* total) {
+int wrach_surrogate_collect(WrachContext* ctx, uint32_t stride, uint32_t* total) {
   int rc = surrogate_ready(ctx);
   if (rc) return rc;
   DeviceGuard guard(ctx->device);
   auto& S = ctx->sur;
-  const uint32_t take = std::min(ctx->n, S.max_samples - S.nsamples);
+  if (stride == 0) stride = 1;
+  wrach::SolveArgs a = solve_args(ctx);
+  // the frame's taking-part particles: every stride-th of them, from an
+  // offset that turns with each call, so that consecutive frames give others
+  uint32_t ntp = 0;
+  if (ctx->n) {
+    CK(cudaMemcpyAsync(&ntp, a.ct + ctx->ncells, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  const uint32_t phase = S.collects++ % stride;
+  const uint32_t rows = ntp > phase ? (ntp - phase + stride - 1) / stride : 0u;
+  const uint32_t take = std::min(rows, S.max_samples - S.nsamples);
   if (take) {
-    wrach::SolveArgs a = solve_args(ctx);
-    // features of the frame, then the correction of its first K-1 iterations
-    CK(wrach::launch_knn_features(a, S.x, ctx->stream));
+    // the features, then the correction of the frame's first K-1 iterations
     const float2* q = nullptr;
     CK(enqueue_iterations(ctx, a, ctx->ph.iterations - 1, ctx->stream, &q, []() {}));
-    CK(wrach::launch_target(a, take, q, S.tt + S.nsamples, ctx->stream));
-    CK(cudaMemcpyAsync(S.tx + (size_t)S.nsamples * wrach::kMlpIn, S.x, (size_t)take * wrach::kMlpIn * 2,
-                       cudaMemcpyDeviceToDevice, ctx->stream));
-    ctx->launches += ctx->ph.iterations + 1;
+    CK(wrach::launch_samples(a, q, stride, phase, take, S.tx + (size_t)S.nsamples * wrach::kMlpIn,
+                             S.tt + S.nsamples, ctx->stream));
+    ctx->launches += ctx->ph.iterations;
     S.nsamples += take;
   }
   if (total) *total = S.nsamples;
@@ -300,8 +339,10 @@ int wrach_surrogate_correction(WrachContext* ctx, float* d_corr) {
   if (!d_corr && ctx->n) return WRACH_ERR_INVALID_ARGUMENT;
   DeviceGuard guard(ctx->device);
   wrach::SolveArgs a = solve_args(ctx);
+  // the particles that take no part get a zero correction
+  if (ctx->n) CK(cudaMemsetAsync(d_corr, 0, (size_t)ctx->n * sizeof(float2), ctx->stream));
   CK(wrach::launch_surrogate_correct(ctx->sur.m, a, ctx->q1, reinterpret_cast<float2*>(d_corr),
-                                     ctx->sur.blocks, ctx->stream));
+                                     ctx->sur.correct_blocks, ctx->stream));
   ctx->launches += ctx->n ? 1 : 0;
   return WRACH_OK;
 }
@@ -344,26 +385,44 @@ int wrach_surrogate_step(WrachContext* ctx, uint32_t nsteps, float max_penetrati
   g0.max_drift = max_energy_drift;
   CK(cudaMemcpyAsync(S.gate, &g0, sizeof(g0), cudaMemcpyHostToDevice, ctx->stream));
   for (uint32_t f = 0; f < nsteps; ++f) {
-    wrach::SolveArgs a = solve_args(ctx);
-    a.part = S.part;
-    const uint32_t nparts = wrach::solve_blocks(a);
-    if (f % kCalibrationPeriod == 0) {
-      // a plain frame: its metrics are the reference of the next frames
-      if ((rc = enqueue_plain_solve(ctx, a))) return rc;
-      CK(wrach::launch_gate(S.part, nparts, S.gate, 2, ctx->stream));
-    } else {
-      // the surrogate correction, the last plain iteration, the gate
-      CK(wrach::launch_surrogate_correct(S.m, a, ctx->q1, nullptr, S.blocks, ctx->stream));
-      CK(wrach::launch_jacobi_final(a, ctx->q1, 1, ctx->stream));
-      CK(wrach::launch_gate(S.part, nparts, S.gate, 0, ctx->stream));
-      // the plain solve of the same frame, run only when the gate failed it
-      a.run_if = &S.gate->fallback;
-      if ((rc = enqueue_plain_solve(ctx, a))) return rc;
-      CK(wrach::launch_gate(S.part, nparts, S.gate, 1, ctx->stream));
-      ctx->launches += 4;
+    const int calibration = f % kCalibrationPeriod == 0 ? 1 : 0;
+    const int parity = ctx->cur;
+    cudaGraphExec_t& g = S.graph[parity][calibration];
+    // a graph holds the particle count (grid sizes) it was captured with
+    if (g && S.graph_n[parity][calibration] != ctx->n) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
     }
-    ctx->launches += 1;
-    if ((rc = enqueue_rebin(ctx))) return rc;
+    if (!g && ctx->graph_ok) {
+      const uint64_t launches = ctx->launches;
+      cudaGraph_t graph = nullptr;
+      bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        rc = enqueue_surrogate_frame(ctx, calibration);
+        ok = cudaStreamEndCapture(ctx->stream, &graph) == cudaSuccess && rc == WRACH_OK && graph;
+        ctx->cur = parity;
+        S.graph_launches[parity][calibration] = (uint32_t)(ctx->launches - launches);
+        ctx->launches = launches;
+        if (ok) ok = cudaGraphInstantiate(&g, graph, 0) == cudaSuccess;
+        if (graph) cudaGraphDestroy(graph);
+      }
+      if (!ok) {
+        // capture unavailable: this and later frames run eagerly
+        cudaGetLastError();
+        g = nullptr;
+        ctx->graph_ok = false;
+        ctx->err.clear();
+      } else {
+        S.graph_n[parity][calibration] = ctx->n;
+      }
+    }
+    if (g) {
+      CK(cudaGraphLaunch(g, ctx->stream));
+      ctx->launches += S.graph_launches[parity][calibration];
+      ctx->cur ^= 1;
+    } else if ((rc = enqueue_surrogate_frame(ctx, calibration))) {
+      return rc;
+    }
   }
   wrach::GateState g{};
   CK(cudaMemcpyAsync(&g, S.gate, sizeof(g), cudaMemcpyDeviceToHost, ctx->stream));

@@ -30,6 +30,8 @@ struct SolveArgs {
   const uint32_t* ct;           // ncells + 1: capped table
   const uint32_t* tp_cell;      // cell of each compacted particle
   const float2* tp_pos;         // compacted positions of the binned state
+  const float2* tp_vel;         // compacted velocities of the binned state
+  int sms;                      // SMs of the device
 };
 
 cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st);
@@ -83,6 +85,7 @@ struct RebinArgs {
   uint32_t* tile_sums_cap;      // per scan tile, its taking-part particles (zero between rebins)
   uint32_t* ct_new;             // ncells + 1: capped table (compacted start of each cell)
   float2* tp_pos;               // compacted positions
+  float2* tp_vel;               // compacted velocities
   uint32_t* tp_cell;            // compacted cells
 };
 
@@ -181,18 +184,26 @@ struct GateState {
 };
 
 cudaError_t launch_knn_features(const SolveArgs& a, uint16_t* x, cudaStream_t st);
+// Training rows of the binned frame: the features of the taking-part
+// particles t = phase + k * stride into rows k of x (at most `rows`) and
+// their targets q_t - p_t from the compacted iterate q.
+cudaError_t launch_samples(const SolveArgs& a, const float2* q, uint32_t stride, uint32_t phase,
+                           uint32_t rows, uint16_t* x, float2* target, cudaStream_t st);
 // Fused surrogate correction of the binned frame: the compacted iterate
 // q_t = p + network(features) of each taking-part particle; `corr` optional
 // (per frame particle).
 cudaError_t launch_surrogate_correct(const MlpDev& m, const SolveArgs& a, float2* q, float2* corr,
                                      int blocks, cudaStream_t st);
+// One-time set-up of the fused correction kernel on `device` (its shared
+// memory size); returns its grid (one wave of co-resident blocks), 0 if the
+// set-up failed.
+int surrogate_correct_blocks(int device);
 cudaError_t launch_gate(const float* part, uint32_t nparts, GateState* gs, int mode,
                         cudaStream_t st);
-// Number of blocks (and so of partials) of an extended solve launch.
-inline uint32_t solve_blocks(const SolveArgs& a) {
-  const uint32_t threads = a.block ? a.block : 128;
-  return (a.n + threads - 1) / threads;
-}
+// Number of blocks (and so of gate partials) of an extended solve launch:
+// one thread per particle, or, for a launch with a run_if flag, a few
+// blocks per SM striding over the frame.
+uint32_t solve_blocks(const SolveArgs& a);
 cudaError_t launch_mlp_forward(const MlpDev& m, const uint16_t* x, uint32_t n, float2* y,
                                int blocks, cudaStream_t st);
 cudaError_t launch_mlp_backward(const MlpDev& m, const uint16_t* x, const float2* target,
