@@ -259,13 +259,21 @@ def run_reference(args):
 # algorithmic bytes of each launch of a frame (n particles, c cells)
 def launch_bytes(kind, n, c):
     if kind == "jacobi":
-        return 20 * n + 4 * c       # q in + q out + cell_of, table once
+        return 20 * n + 4 * c       # q in + q out + cell, capped table once (all take part)
     if kind == "jacobi_final":
         return 40 * n + 4 * c       # q, vel, cell_of in; pos, vel, key out
     if kind == "solve_reference":
         return 36 * n + 4 * c       # pos, vel in; pos, vel, key out
     if kind == "rebin":
         return 40 * n + 8 * c       # key, pos, vel in; pos, vel, cell_of out; table in + out
+    if kind == "rebin_count":
+        return 8 * n                # keys in, tickets out
+    if kind == "rebin_scan":
+        return 16 * c               # counts in and cleared, both tables out
+    if kind == "rebin_scatter":
+        return 20 * n               # keys, tickets, starts in; source and cell out
+    if kind == "rebin_place":
+        return 64 * n               # slots in; pos, vel in; pos, vel, cell and compacted copies out
     return 0
 
 
@@ -365,8 +373,12 @@ def run_ours(args):
     for k, ms in zip(solve_kinds, prof):
         per_kind.setdefault(k, []).append(ms)
     rebin_steps = {s: float(ms) for s, ms in zip(rebin_kinds, prof[len(solve_kinds):])}
-    per_kind["rebin"] = [float(sum(rebin_steps.values()))]
+    # the dominant kernel: the most time per frame of one kernel (the
+    # rebin's launches each count on their own)
+    for step, ms in rebin_steps.items():
+        per_kind["rebin_" + step] = [ms]
     dom = max(per_kind, key=lambda k: sum(per_kind[k]))
+    per_kind["rebin"] = [float(sum(rebin_steps.values()))]
     dom_ms = statistics.mean(per_kind[dom])
     peak, peak_kind = measured_peak()
     achieved = launch_bytes(dom, n, cells) / (dom_ms / 1000.0) / 1e9

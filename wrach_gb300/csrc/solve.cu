@@ -327,7 +327,7 @@ uint32_t solve_blocks(const SolveArgs& a) {
   const uint32_t blocks = (a.n + threads - 1) / threads;
   // a launch that usually returns at once (the surrogate's fallback) strides
   // over the frame with a few blocks per SM, so that skipping it is cheap
-  const uint32_t few = 4u * (uint32_t)(a.sms > 0 ? a.sms : 1) * (512u / threads);
+  const uint32_t few = (uint32_t)(a.sms > 0 ? a.sms : 1) * (1024u / threads);
   return a.run_if && blocks > few ? few : blocks;
 }
 

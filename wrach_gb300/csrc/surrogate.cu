@@ -843,6 +843,8 @@ k_penetration(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint
 __global__ void __launch_bounds__(256)
 k_reduce_partials(const float* __restrict__ part, uint32_t nparts, float* __restrict__ out) {
   float v[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  // unrolled, so that the loads of several partials are in flight at once
+#pragma unroll 4
   for (uint32_t b = threadIdx.x; b < nparts; b += blockDim.x) {
 #pragma unroll
     for (int k = 0; k < 5; ++k) v[k] = k == 1 ? fmaxf(v[k], part[b * 8 + k]) : v[k] + part[b * 8 + k];
@@ -861,10 +863,12 @@ k_reduce_partials(const float* __restrict__ part, uint32_t nparts, float* __rest
 //   1  after the (gated) fallback solve: when the frame fell back, its plain
 //      metrics become the reference;
 //   2  after a plain calibration frame: its metrics become the reference.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(1024)
 k_gate(const float* __restrict__ part, uint32_t nparts, GateState* __restrict__ gs, int mode) {
   if (mode == 1 && gs->fallback == 0u) return;
   float v[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  // unrolled, so that the loads of several partials are in flight at once
+#pragma unroll 4
   for (uint32_t b = threadIdx.x; b < nparts; b += blockDim.x) {
 #pragma unroll
     for (int k = 0; k < 5; ++k) v[k] = k == 1 ? fmaxf(v[k], part[b * 8 + k]) : v[k] + part[b * 8 + k];
@@ -976,7 +980,7 @@ cudaError_t launch_surrogate_correct(const MlpDev& m, const SolveArgs& a, float2
 
 cudaError_t launch_gate(const float* part, uint32_t nparts, GateState* gs, int mode,
                         cudaStream_t st) {
-  k_gate<<<1, 256, 0, st>>>(part, nparts, gs, mode);
+  k_gate<<<1, 1024, 0, st>>>(part, nparts, gs, mode);
   return cudaGetLastError();
 }
 
