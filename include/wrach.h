@@ -308,9 +308,16 @@ int wrach_surrogate_set_params(WrachContext *ctx, const float *params,
 /* Features of the current frame (BF16 rows of 64) into a device buffer of
  * at least particles_in_frame rows. */
 int wrach_surrogate_features(WrachContext *ctx, uint16_t *d_x, uint32_t rows);
-/* Network outputs (n float pairs) of n device feature rows. */
+/* Network outputs (n float pairs) of n device feature rows, on the tcgen05
+ * tensor cores (operands in shared memory, accumulators in tensor memory).
+ * Asynchronous; a bounded device wait that gives up raises
+ * WRACH_FLAG_TIMEOUT (wrach_flags). */
 int wrach_surrogate_forward(WrachContext *ctx, const uint16_t *d_x,
                             uint32_t n, float *d_y);
+/* The same on the warp-level mma.sync tensor-core instructions (the kernel
+ * the fused correction of surrogate frames and the training run on). */
+int wrach_surrogate_forward_mma(WrachContext *ctx, const uint16_t *d_x,
+                                uint32_t n, float *d_y);
 /* Gradients (host, param_count floats) and loss of 0.5 * mean over the n
  * rows of the squared error against d_t (n float pairs). */
 int wrach_surrogate_gradients(WrachContext *ctx, const uint16_t *d_x,

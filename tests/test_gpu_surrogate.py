@@ -65,19 +65,44 @@ def test_forward_and_gradients_match_oracle(W):
         dx = torch.from_numpy((M.bf16_bits(x).astype(np.uint16)).view(np.int16)).cuda()
         dt = torch.from_numpy(t).cuda()
         dy = torch.zeros((n, 2), dtype=torch.float32, device="cuda")
-        sim.surrogate_forward(dx.data_ptr(), n, dy.data_ptr())
-        sim.sync()
-        y_gpu = dy.cpu().numpy()
         y_cpu, _ = M.forward(params, x)
-        # BF16 activations: an FP32 vs float64 accumulation can flip an
-        # activation's BF16 rounding, one BF16 ulp (2^-8 relative)
-        assert np.abs(y_gpu - y_cpu).max() <= 2e-2 * np.abs(y_cpu).max()
+        for kernel in ("tcgen05", "mma"):
+            dy.zero_()
+            sim.surrogate_forward(dx.data_ptr(), n, dy.data_ptr(), kernel=kernel)
+            sim.sync()
+            y_gpu = dy.cpu().numpy()
+            # BF16 activations: an FP32 vs float64 accumulation can flip an
+            # activation's BF16 rounding, one BF16 ulp (2^-8 relative)
+            assert np.abs(y_gpu - y_cpu).max() <= 2e-2 * np.abs(y_cpu).max(), kernel
+        assert sim.flags() == 0
         g_gpu, l_gpu = sim.surrogate_gradients(dx.data_ptr(), dt.data_ptr(), n)
         g_cpu, l_cpu = M.gradients(params, x, t)
         assert abs(l_gpu - l_cpu) <= 1e-2 * l_cpu
         for name, a, b in zip(("w1", "b1", "w2", "b2", "w3", "b3"), M.unpack(g_gpu), M.unpack(g_cpu)):
             err = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
             assert err < 3e-2, (name, err)
+
+
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 70001])
+def test_tcgen05_forward_matches_mma_forward(W, n):
+    # the tcgen05 kernel (tiles of 128 rows, accumulators in tensor memory)
+    # against the mma.sync kernel on the same rows, ragged last tiles included
+    torch = _torch()
+    rng = np.random.default_rng(7 + n)
+    with _sim(W, (30.0, 30.0), 100) as sim:
+        sim.surrogate_init(0, 16)
+        sim.surrogate_set_params(_random_net(rng))
+        x = M.bf16(rng.normal(0, 0.7, (n, 64)).astype(np.float32))
+        dx = torch.from_numpy((M.bf16_bits(x).astype(np.uint16)).view(np.int16)).cuda()
+        ya = torch.full((n + 1, 2), 7.0, dtype=torch.float32, device="cuda")
+        yb = torch.full((n + 1, 2), 7.0, dtype=torch.float32, device="cuda")
+        sim.surrogate_forward(dx.data_ptr(), n, ya.data_ptr(), kernel="tcgen05")
+        sim.surrogate_forward(dx.data_ptr(), n, yb.data_ptr(), kernel="mma")
+        sim.sync()
+        a, b = ya.cpu().numpy(), yb.cpu().numpy()
+        assert np.all(a[n] == 7.0)  # nothing written past the rows
+        assert np.abs(a[:n] - b[:n]).max() <= 2e-2 * max(np.abs(b[:n]).max(), 1e-3)
+        assert sim.flags() == 0
 
 
 def test_training_beats_the_frame_without_the_network(W):
@@ -167,7 +192,9 @@ def test_fused_correction_matches_the_separate_kernels(W):
         y = torch.zeros((n, 2), dtype=torch.float32, device="cuda")
         c = torch.full((n, 2), 7.0, dtype=torch.float32, device="cuda")
         sim.surrogate_features(x.data_ptr(), n)
-        sim.surrogate_forward(x.data_ptr(), n, y.data_ptr())
+        # the fused pass runs the mma.sync network: the same products in the
+        # same order as that forward kernel
+        sim.surrogate_forward(x.data_ptr(), n, y.data_ptr(), kernel="mma")
         sim.surrogate_correction(c.data_ptr())
         sim.sync()
         start = np.asarray(table, np.int64)[1:]

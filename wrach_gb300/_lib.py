@@ -121,6 +121,7 @@ SIGNATURES = {
     "wrach_surrogate_set_params": (ctypes.c_int, [_P, _F, ctypes.c_uint32]),
     "wrach_surrogate_features": (ctypes.c_int, [_P, _P, ctypes.c_uint32]),
     "wrach_surrogate_forward": (ctypes.c_int, [_P, _P, ctypes.c_uint32, _P]),
+    "wrach_surrogate_forward_mma": (ctypes.c_int, [_P, _P, ctypes.c_uint32, _P]),
     "wrach_surrogate_gradients": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _F, _F]),
     "wrach_surrogate_collect": (ctypes.c_int, [_P, ctypes.c_uint32, _U]),
     "wrach_surrogate_evaluate": (ctypes.c_int, [_P, _F, _F]),

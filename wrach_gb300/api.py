@@ -242,9 +242,12 @@ class Simulation:
     def surrogate_features(self, d_x, rows):
         self._check(self._L.wrach_surrogate_features(self._ctx, ctypes.c_void_p(d_x), int(rows)))
 
-    def surrogate_forward(self, d_x, n, d_y):
-        self._check(self._L.wrach_surrogate_forward(self._ctx, ctypes.c_void_p(d_x), int(n),
-                                                    ctypes.c_void_p(d_y)))
+    def surrogate_forward(self, d_x, n, d_y, kernel="tcgen05"):
+        """Network outputs of n device feature rows into d_y; kernel
+        "tcgen05" (tensor memory accumulators) or "mma" (warp-level mma.sync)."""
+        fn = (self._L.wrach_surrogate_forward if kernel == "tcgen05"
+              else self._L.wrach_surrogate_forward_mma)
+        self._check(fn(self._ctx, ctypes.c_void_p(d_x), int(n), ctypes.c_void_p(d_y)))
 
     def surrogate_gradients(self, d_x, d_t, n):
         g = np.empty(int(self._L.wrach_surrogate_param_count()), np.float32)

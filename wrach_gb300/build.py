@@ -27,8 +27,10 @@ NVCC_FLAGS = ARCH + [
 # The network kernels are checked against the oracle within a BF16
 # tolerance, not bit for bit, so they may contract multiply-adds; the parts of
 # surrogate.cu that must be exact (features, overlaps) round each operation
-# explicitly (__fmul_rn / __fadd_rn are never contracted).
-FILE_FLAGS = {"surrogate.cu": {"-fmad=false": "-fmad=true"}}
+# explicitly (__fmul_rn / __fadd_rn are never contracted).  mlp_tc.cu is the
+# network alone.
+FILE_FLAGS = {"surrogate.cu": {"-fmad=false": "-fmad=true"},
+              "mlp_tc.cu": {"-fmad=false": "-fmad=true"}}
 
 
 def flags_for(src):

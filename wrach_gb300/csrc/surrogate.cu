@@ -8,7 +8,8 @@
 //             (dx, dy, dvx, dvy) relative to the particle, then the
 //             particle's own velocity; 50 values padded to 64, BF16.
 //   network   64 -> 64 -> 64 -> 2 (padded to 8), GELU (tanh form) after the
-//             two hidden layers; BF16 weights, FP32 accumulation, on the
+//             two hidden layers (inference evaluates it on packed FP16 pairs,
+//             gelu.cuh); BF16 weights, FP32 accumulation, on the
 //             tensor cores with mma.sync m16n8k16 (one warp per 16 rows; the
 //             accumulator fragment of one layer is the A fragment of the
 //             next, so the layers chain in registers).
@@ -19,6 +20,7 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include "gelu.cuh"
 #include "wrach_internal.cuh"
 #include "wrach_kernels.h"
 
@@ -184,9 +186,10 @@ __device__ __forceinline__ uint32_t lds_keep(const uint32_t* p) {
   return v;
 }
 
-// The forward pass of a 16-row tile for inference only: the same products
-// in the same order as mlp_tile_forward (bit-identical outputs), computed two
-// n-tiles at a time so that no pre-activation array stays live.
+// The forward pass of a 16-row tile for inference only: the same products in
+// the same order as mlp_tile_forward, computed two n-tiles at a time so that
+// no pre-activation array stays live, with the GELU on packed FP16 pairs
+// (gelu2_bf16; the training pass keeps the FP32 GELU and its derivative).
 __device__ __forceinline__ void mlp_tile_infer(const SmemNet& s, uint32_t lane,
                                                const uint32_t (&ax)[4][4], float (&y)[4]) {
   const uint32_t g = lane >> 2, t = lane & 3;
@@ -204,10 +207,10 @@ __device__ __forceinline__ void mlp_tile_infer(const SmemNet& s, uint32_t lane,
       for (uint32_t kk = 0; kk < 4; ++kk)
         mma_bf16(z[u], ax[kk], lds_keep(row + kk * 8), lds_keep(row + kk * 8 + 4));
     }
-    h1[kq][0] = pack_bf16(gelu(z[0][0]), gelu(z[0][1]));
-    h1[kq][1] = pack_bf16(gelu(z[0][2]), gelu(z[0][3]));
-    h1[kq][2] = pack_bf16(gelu(z[1][0]), gelu(z[1][1]));
-    h1[kq][3] = pack_bf16(gelu(z[1][2]), gelu(z[1][3]));
+    h1[kq][0] = gelu2_bf16(z[0][0], z[0][1]);
+    h1[kq][1] = gelu2_bf16(z[0][2], z[0][3]);
+    h1[kq][2] = gelu2_bf16(z[1][0], z[1][1]);
+    h1[kq][3] = gelu2_bf16(z[1][2], z[1][3]);
   }
 #pragma unroll
   for (uint32_t kq = 0; kq < 4; ++kq) {
@@ -222,10 +225,10 @@ __device__ __forceinline__ void mlp_tile_infer(const SmemNet& s, uint32_t lane,
       for (uint32_t kk = 0; kk < 4; ++kk)
         mma_bf16(z[u], h1[kk], lds_keep(row + kk * 8), lds_keep(row + kk * 8 + 4));
     }
-    h2[kq][0] = pack_bf16(gelu(z[0][0]), gelu(z[0][1]));
-    h2[kq][1] = pack_bf16(gelu(z[0][2]), gelu(z[0][3]));
-    h2[kq][2] = pack_bf16(gelu(z[1][0]), gelu(z[1][1]));
-    h2[kq][3] = pack_bf16(gelu(z[1][2]), gelu(z[1][3]));
+    h2[kq][0] = gelu2_bf16(z[0][0], z[0][1]);
+    h2[kq][1] = gelu2_bf16(z[0][2], z[0][3]);
+    h2[kq][2] = gelu2_bf16(z[1][0], z[1][1]);
+    h2[kq][3] = gelu2_bf16(z[1][2], z[1][3]);
   }
   const float bl = s.b3[2 * t], bh = s.b3[2 * t + 1];
   y[0] = bl; y[1] = bh; y[2] = bl; y[3] = bh;

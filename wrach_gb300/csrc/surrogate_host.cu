@@ -236,6 +236,17 @@ int wrach_surrogate_forward(WrachContext* ctx, const uint16_t* d_x, uint32_t n, 
   if (rc) return rc;
   if (n && (!d_x || !d_y)) return WRACH_ERR_INVALID_ARGUMENT;
   DeviceGuard guard(ctx->device);
+  CK(wrach::launch_mlp_forward_tc(ctx->sur.m, d_x, n, reinterpret_cast<float2*>(d_y),
+                                  &ctx->ctrl->flags, ctx->sms, ctx->stream));
+  ctx->launches += n ? 1 : 0;
+  return WRACH_OK;
+}
+
+int wrach_surrogate_forward_mma(WrachContext* ctx, const uint16_t* d_x, uint32_t n, float* d_y) {
+  int rc = surrogate_ready(ctx);
+  if (rc) return rc;
+  if (n && (!d_x || !d_y)) return WRACH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(ctx->device);
   CK(wrach::launch_mlp_forward(ctx->sur.m, d_x, n, reinterpret_cast<float2*>(d_y), ctx->sur.blocks,
                                ctx->stream));
   ctx->launches += n ? 1 : 0;

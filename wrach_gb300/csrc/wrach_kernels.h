@@ -206,6 +206,11 @@ cudaError_t launch_gate(const float* part, uint32_t nparts, GateState* gs, int m
 uint32_t solve_blocks(const SolveArgs& a);
 cudaError_t launch_mlp_forward(const MlpDev& m, const uint16_t* x, uint32_t n, float2* y,
                                int blocks, cudaStream_t st);
+// The same forward pass on the tcgen05 tensor cores (mlp_tc.cu): operands in
+// shared memory, accumulators in TMEM; a bounded wait that gives up raises
+// kFlagTimeout in *flags.
+cudaError_t launch_mlp_forward_tc(const MlpDev& m, const uint16_t* x, uint32_t n, float2* y,
+                                  uint32_t* flags, int sms, cudaStream_t st);
 cudaError_t launch_mlp_backward(const MlpDev& m, const uint16_t* x, const float2* target,
                                 uint32_t n, float inv_rows, float* grad, float* loss,
                                 int blocks, cudaStream_t st);
