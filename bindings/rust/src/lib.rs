@@ -41,7 +41,8 @@ pub struct WrachConfigC {
     pub device: i32,
     pub rebin_blocks: u32,
     pub solve_block: u32,
-    pub reserved: [u32; 5],
+    pub solve_per_thread: u32,
+    pub reserved: [u32; 4],
 }
 
 #[repr(C)]

@@ -82,7 +82,10 @@ typedef struct WrachConfig {
                               more than 64 particles), 0 = 8 per SM */
   uint32_t solve_block;    /* threads per block of the solve kernels, a
                               multiple of 32 up to 512, 0 = 128 */
-  uint32_t reserved[5];
+  uint32_t solve_per_thread; /* particles each thread of the extended solve
+                              takes in turn (the grid shrinks accordingly;
+                              32 x this = particles per warp), 0 = 1 */
+  uint32_t reserved[4];
 } WrachConfig;
 
 typedef struct WrachContext WrachContext;

@@ -1,4 +1,6 @@
 """The autotuner's cache (CPU) and a small tuning run (GPU)."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -27,13 +29,17 @@ def test_tune_picks_a_candidate_and_caches_it(W, tmp_path):
     cfg = W.WrachConfig(dimensions=dims, cell_size=1, mode=1, iterations=2, gravity=0.1,
                         capacity=20000)
     path = str(tmp_path / "tune.json")
-    tuned, ms = autotune.tune(cfg, pos, vel, frames=4, solve_blocks=(128, 256), path=path)
-    assert tuned.solve_block in (128, 256) and tuned.rebin_blocks > 0
-    assert len(ms) >= 2 and all(v > 0 for v in ms.values())
-    again, ms2 = autotune.tune(cfg, pos, vel, frames=4, solve_blocks=(128, 256), path=path)
+    tuned, ms = autotune.tune(cfg, pos, vel, frames=4, solve_blocks=(128, 256), per_thread=(1, 3),
+                              path=path)
+    assert tuned.solve_block in (128, 256) and tuned.solve_per_thread in (1, 3)
+    assert tuned.rebin_blocks > 0
+    assert len(ms) >= 6 and all(v > 0 for v in ms.values())
+    again, ms2 = autotune.tune(cfg, pos, vel, frames=4, solve_blocks=(128, 256), per_thread=(1, 3),
+                               path=path)
     assert again == tuned and ms2 == ms
-    # the tuned launch shape does not change results
-    with W.Simulation(cfg) as a, W.Simulation(tuned) as b:
+    # a launch shape does not change results
+    odd = dataclasses.replace(cfg, solve_block=96, solve_per_thread=5)
+    with W.Simulation(cfg) as a, W.Simulation(odd) as b:
         a.add_particles(pos, vel)
         b.add_particles(pos, vel)
         a.step(5)

@@ -66,7 +66,8 @@ class Config(ctypes.Structure):
                 ("device", ctypes.c_int32),
                 ("rebin_blocks", ctypes.c_uint32),
                 ("solve_block", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 5)]
+                ("solve_per_thread", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 4)]
 
 
 class Stats(ctypes.Structure):

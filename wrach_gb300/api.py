@@ -51,6 +51,7 @@ class WrachConfig:
     device: int = 0
     rebin_blocks: int = 0
     solve_block: int = 0
+    solve_per_thread: int = 0
 
     def to_c(self):
         c = _lib.Config()
@@ -68,6 +69,7 @@ class WrachConfig:
         c.device = int(self.device)
         c.rebin_blocks = int(self.rebin_blocks)
         c.solve_block = int(self.solve_block)
+        c.solve_per_thread = int(self.solve_per_thread)
         return c
 
 

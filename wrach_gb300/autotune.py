@@ -6,9 +6,12 @@ assets/shaders/prefix_sum.wgsl:9-15) and lists changing them as a TODO
 (README.md:28).  Here the launch shape is a per-context setting, and `tune`
 picks it by timing candidates on the workload itself:
 
-  solve_block    threads per block of the solve kernels
-  rebin_blocks   the grid of the rebin's large-cell sort (its blocks loop
-                 over the cells of more than 64 particles; default 8 per SM)
+  solve_block       threads per block of the solve kernels
+  solve_per_thread  particles each thread of the extended solve takes in
+                    turn (32 x this = particles per warp); the grid shrinks
+                    by the same factor
+  rebin_blocks      the grid of the rebin's large-cell sort (its blocks loop
+                    over the cells of more than 64 particles; default 8 per SM)
   cell_size      only when the caller passes `cell_sizes`: it is a physics
                  change, not a launch shape -- it changes which particles
                  share a cell, hence the capacity rule and the summation order
@@ -92,7 +95,7 @@ def _time_frames(sim, frames):
     return (time.perf_counter() - t0) * 1000.0 / frames
 
 
-LAUNCH_KNOBS = ("solve_block", "rebin_blocks")
+LAUNCH_KNOBS = ("solve_block", "solve_per_thread", "rebin_blocks")
 
 
 def launch_shape(config):
@@ -101,12 +104,15 @@ def launch_shape(config):
 
 
 def tune(config, positions, velocities, worlds=None, frames=10, rebin_blocks=None,
-         solve_blocks=(128, 256, 512), cell_sizes=None, use_cache=True, path=None):
+         solve_blocks=(128, 256, 512), per_thread=(1, 2, 4), cell_sizes=None, use_cache=True,
+         path=None):
     """Returns (tuned config, {candidate: ms per frame}).  `positions` and
     `velocities` are one (n, 2) array each, or one per world when `worlds`
-    (a list of (width, height)) is given.  `rebin_blocks` defaults to 4, 8
-    and 16 blocks per SM.  `cell_sizes` (e.g. (1, 2)) lets the tuner change
-    the cell size, which changes the physics."""
+    (a list of (width, height)) is given.  For each cell size, the solve's
+    block size and particles per thread are tuned together, then the
+    rebin's large-cell grid (`rebin_blocks`, default 4, 8 and 16 blocks per
+    SM) for the best of those.  `cell_sizes` (e.g. (1, 2)) lets the tuner
+    change the cell size, which changes the physics."""
     tune_cs = bool(cell_sizes)
     cell_sizes = tuple(cell_sizes) if cell_sizes else (config.cell_size,)
     probe = api.Simulation(dataclasses.replace(config), worlds=worlds)
@@ -123,18 +129,28 @@ def tune(config, positions, velocities, worlds=None, frames=10, rebin_blocks=Non
     if rebin_blocks is None:
         rebin_blocks = (per_sm8 // 2, per_sm8, per_sm8 * 2)
     timings = {}
+
+    def run(**knobs):
+        cand = dataclasses.replace(config, **knobs)
+        with api.Simulation(cand, worlds=worlds) as sim:
+            _upload(sim, positions, velocities, worlds)
+            ms = _time_frames(sim, frames)
+        label = ",".join("%s=%d" % (k, knobs[k]) for k in ("cell_size",) + LAUNCH_KNOBS)
+        timings[label] = ms
+        return ms
+
     best, best_ms = None, float("inf")
     for cs in cell_sizes:
+        shape, shape_ms = None, float("inf")
+        for sb in solve_blocks:
+            for pt in per_thread:
+                ms = run(cell_size=cs, solve_block=sb, solve_per_thread=pt, rebin_blocks=per_sm8)
+                if ms < shape_ms:
+                    shape_ms, shape = ms, dict(cell_size=cs, solve_block=sb, solve_per_thread=pt)
         for rb in rebin_blocks:
-            for sb in solve_blocks:
-                cand = dataclasses.replace(config, cell_size=cs, rebin_blocks=rb, solve_block=sb)
-                with api.Simulation(cand, worlds=worlds) as sim:
-                    _upload(sim, positions, velocities, worlds)
-                    ms = _time_frames(sim, frames)
-                label = "cs=%d,rebin_blocks=%d,solve_block=%d" % (cs, rb, sb)
-                timings[label] = ms
-                if ms < best_ms:
-                    best_ms, best = ms, dict(cell_size=cs, rebin_blocks=rb, solve_block=sb)
+            ms = shape_ms if rb == per_sm8 else run(rebin_blocks=rb, **shape)
+            if ms < best_ms:
+                best_ms, best = ms, dict(shape, rebin_blocks=rb)
     if use_cache:
         cache[key] = {"choice": best, "ms": timings}
         save_cache(cache, path)

@@ -204,6 +204,7 @@ wrach::SolveArgs solve_args(WrachContext* ctx) {
   a.keys = ctx->keys;
   a.ctrl = ctx->ctrl;
   a.block = ctx->cfg.solve_block;
+  a.per_thread = ctx->cfg.solve_per_thread;
   a.ct = ctx->ct[ctx->cur];
   a.tp_cell = ctx->tp_cell[ctx->cur];
   a.tp_pos = ctx->tp_pos[ctx->cur];
@@ -307,7 +308,7 @@ int enqueue_frame(WrachContext* ctx) {
     CK(wrach::launch_count_sort_step(r, step, ctx->big_blocks, st, &launched));
     if (launched) mark(ctx);
   }
-  ctx->launches += wrach::count_sort_launches(r.n) - (tickets_taken && r.n ? 1 : 0);
+  ctx->launches += wrach::count_sort_launches(r.n, ctx->ncells) - (tickets_taken && r.n ? 1 : 0);
   ctx->cur ^= 1;
   return WRACH_OK;
 }
@@ -316,15 +317,16 @@ int enqueue_frame(WrachContext* ctx) {
 // each rebin launch (an empty frame's extended solve launches nothing, but
 // still marks its steps).
 uint32_t frame_steps(const WrachContext* ctx) {
-  const uint32_t rebin = wrach::count_sort_launches(ctx->n);
+  const uint32_t rebin = wrach::count_sort_steps(ctx->n);
   if (ctx->ph.mode == WRACH_MODE_REFERENCE) return 1 + rebin;
   return std::max<uint32_t>(ctx->ph.iterations, 1) + rebin - (ctx->n ? 1 : 0);
 }
 
 // Kernel launches of one frame.
 uint32_t frame_launches(const WrachContext* ctx) {
-  if (ctx->ph.mode == WRACH_MODE_EXTENDED && !ctx->n) return wrach::count_sort_launches(0);
-  return frame_steps(ctx);
+  const uint32_t extra = wrach::count_sort_launches(ctx->n, ctx->ncells) - wrach::count_sort_steps(ctx->n);
+  if (ctx->ph.mode == WRACH_MODE_EXTENDED && !ctx->n) return wrach::count_sort_launches(0, ctx->ncells);
+  return frame_steps(ctx) + extra;
 }
 
 // One frame captured as a CUDA graph, instantiated once per table parity
@@ -412,6 +414,7 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   if (c.iterations > 64) return bad("iterations must be at most 64");
   if (c.solve_block && (c.solve_block > 512 || c.solve_block % 32))
     return bad("solve_block must be a multiple of 32 up to 512");
+  if (c.solve_per_thread > 64) return bad("solve_per_thread must be at most 64");
 
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -621,7 +624,7 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
   r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
   r.force_general = 1;
   CK(wrach::launch_count_sort(r, ctx->big_blocks, ctx->stream));
-  ctx->launches += wrach::count_sort_launches(r.n);
+  ctx->launches += wrach::count_sort_launches(r.n, ctx->ncells);
 
   // per-world counts from the new table
   const uint32_t nw = ctx->nworlds;

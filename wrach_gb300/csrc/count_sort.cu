@@ -12,12 +12,15 @@
 //            in its last Jacobi pass instead (the keys are computed there)
 //   scan     exclusive scan of the per-cell counts, one block per tile of
 //            2048 cells; a tile's prefix is the sum of the earlier tiles'
-//            sums (already final, so no block waits); it writes the
+//            sums (already final, so no block waits): each block adds them
+//            up itself, or, past kPrefixTiles tiles (where that sum grows
+//            with the square of the grid), a one-block launch first turns
+//            the tile sums into their prefixes; it writes the
 //            cell-start table and (extended physics) the capped table of the
 //            taking-part particles from the counts capped at the cell
-//            capacity, clears the counts and lists the cells of more than
-//            kSmallCell particles (the pass that takes the tickets empties
-//            that list first)
+//            capacity, and lists the cells of more than kSmallCell particles
+//            (the pass that takes the tickets empties that list first); the
+//            place steps clear the counts of the non-empty cells afterwards
 //   scatter  source index and cell of every particle to table start + ticket
 //            (arrival order inside a cell)
 //   place    the stable order: inside a cell, a particle's rank is the number
@@ -76,6 +79,55 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* red) {
 // One block per tile of 2048 cells.  The tile's prefix is the sum of the
 // earlier tiles' counts, which the tickets' pass has already totalled, so no
 // block waits for another.
+// Past this many tiles of the table, the tile sums are turned into prefixes
+// by k_cs_tile_prefix first.
+constexpr uint32_t kPrefixTiles = 2048;
+
+// One block of 1024 threads: the tile sums (and the capped ones) replaced by
+// their exclusive prefixes, in place; each thread scans a contiguous run.
+__global__ void __launch_bounds__(1024) k_cs_tile_prefix(RebinArgs a, uint32_t ntiles) {
+  __shared__ uint32_t ws[32], wc[32];
+  const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const uint32_t per = (ntiles + 1023) / 1024;
+  const uint32_t i0 = min(t * per, ntiles), i1 = min(i0 + per, ntiles);
+  const bool cap = a.tp_cap != 0u;
+  uint32_t s = 0, c = 0;
+  for (uint32_t i = i0; i < i1; ++i) {
+    s += __ldcg(a.tile_sums + i);
+    if (cap) c += __ldcg(a.tile_sums_cap + i);
+  }
+  uint32_t x = s, y = c;
+#pragma unroll
+  for (uint32_t o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, x, o), v = __shfl_up_sync(0xffffffffu, y, o);
+    if (lane >= o) {
+      x += u;
+      y += v;
+    }
+  }
+  if (lane == 31) {
+    ws[warp] = x;
+    wc[warp] = y;
+  }
+  __syncthreads();
+  uint32_t bs = 0, bc = 0;
+  for (uint32_t w = 0; w < warp; ++w) {
+    bs += ws[w];
+    bc += wc[w];
+  }
+  uint32_t run = bs + x - s, crun = bc + y - c;
+  for (uint32_t i = i0; i < i1; ++i) {
+    const uint32_t v = __ldcg(a.tile_sums + i);
+    a.tile_sums[i] = run;
+    run += v;
+    if (cap) {
+      const uint32_t w = __ldcg(a.tile_sums_cap + i);
+      a.tile_sums_cap[i] = crun;
+      crun += w;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
   __shared__ uint32_t warp_sum[kScanThreads / 32], red[kScanThreads / 32];
   __shared__ uint32_t warp_cap[kScanThreads / 32];
@@ -104,13 +156,19 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
     csum += min(v[u], cap);
   }
   // the earlier tiles' totals
-  uint32_t pre = 0, cpre = 0;
-  for (uint32_t u = t; u < tile; u += kScanThreads) {
-    pre += __ldcg(a.tile_sums + u);
-    if (cap) cpre += __ldcg(a.tile_sums_cap + u);
+  uint32_t prefix, cprefix;
+  if (a.tiles_prefixed) {
+    prefix = __ldcg(a.tile_sums + tile);
+    cprefix = cap ? __ldcg(a.tile_sums_cap + tile) : 0u;
+  } else {
+    uint32_t pre = 0, cpre = 0;
+    for (uint32_t u = t; u < tile; u += kScanThreads) {
+      pre += __ldcg(a.tile_sums + u);
+      if (cap) cpre += __ldcg(a.tile_sums_cap + u);
+    }
+    prefix = block_sum(pre, red);
+    cprefix = cap ? block_sum(cpre, red) : 0u;
   }
-  const uint32_t prefix = block_sum(pre, red);
-  const uint32_t cprefix = cap ? block_sum(cpre, red) : 0u;
   // block-wide exclusive scans of the per-thread sums
   uint32_t x = sum, cx = csum;
 #pragma unroll
@@ -170,7 +228,6 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
   }
   if (c0 + kScanPer <= n) {
     uint4* dst = reinterpret_cast<uint4*>(a.cs_new + c0);
-    uint4* cnt = reinterpret_cast<uint4*>(a.counts + c0);
 #pragma unroll
     for (uint32_t u = 0; u < kScanPer / 4; ++u) {
       uint4 q;
@@ -179,15 +236,11 @@ __global__ void __launch_bounds__(kScanThreads) k_cs_scan(RebinArgs a) {
       q.z = run; run += v[4 * u + 2];
       q.w = run; run += v[4 * u + 3];
       dst[u] = q;
-      cnt[u] = make_uint4(0u, 0u, 0u, 0u);
     }
   } else {
 #pragma unroll
     for (uint32_t u = 0; u < kScanPer; ++u) {
-      if (c0 + u < n) {
-        a.cs_new[c0 + u] = run;
-        a.counts[c0 + u] = 0u;
-      }
+      if (c0 + u < n) a.cs_new[c0 + u] = run;
       run += v[u];
     }
   }
@@ -253,6 +306,9 @@ __global__ void __launch_bounds__(256) k_cs_place(RebinArgs a) {
     uint32_t rank = 0;
     for (uint32_t m = c0; m < s1; ++m) rank += a.idx_tmp[m] < me ? 1u : 0u;
     place_one(a, c0 + rank, rank, me, k, overflow);
+    // the scan has read the cell's count: zero for the next rebin (only
+    // non-empty cells were counted)
+    if (rank == 0) a.counts[k] = 0u;
   }
   add_overflow(a, overflow);
 }
@@ -330,6 +386,7 @@ __global__ void __launch_bounds__(kBigThreads) k_cs_big(RebinArgs a) {
   for (uint32_t w = blockIdx.x; w < nb; w += gridDim.x) {
     const uint32_t k = a.big_list[w];
     const uint32_t s0 = a.cs_new[k], s1 = min(a.cs_new[k + 1], a.n);
+    if (threadIdx.x == 0) a.counts[k] = 0u;  // read by the scan; zero for the next rebin
     const uint32_t s = s1 > s0 ? s1 - s0 : 0u;
     if (s > kBigCell) {
       const uint32_t* sorted = block_radix_sort(a.idx_tmp + s0, a.idx_alt + s0, s, key_bits);
@@ -377,7 +434,14 @@ cudaError_t launch_count_sort_step(const RebinArgs& a, int step, uint32_t big_bl
     }
     k_cs_count<<<nblk, 256, 0, st>>>(a);
   } else if (step == 1) {
-    k_cs_scan<<<ntiles ? ntiles : 1u, kScanThreads, 0, st>>>(a);
+    RebinArgs b = a;
+    b.tiles_prefixed = ntiles > kPrefixTiles ? 1u : 0u;
+    if (b.tiles_prefixed) {
+      k_cs_tile_prefix<<<1, 1024, 0, st>>>(b, ntiles);
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    k_cs_scan<<<ntiles ? ntiles : 1u, kScanThreads, 0, st>>>(b);
   } else if (!nblk) {
     *launched = false;
     return cudaSuccess;
@@ -400,6 +464,11 @@ cudaError_t launch_count_sort(const RebinArgs& a, uint32_t big_blocks, cudaStrea
   return cudaSuccess;
 }
 
-uint32_t count_sort_launches(uint32_t n) { return n ? 5u : 1u; }
+uint32_t count_sort_steps(uint32_t n) { return n ? 5u : 1u; }
+
+uint32_t count_sort_launches(uint32_t n, uint32_t ncells) {
+  const uint32_t ntiles = (ncells + kScanTile - 1) / kScanTile;
+  return count_sort_steps(n) + (ntiles > kPrefixTiles ? 1u : 0u);
+}
 
 }  // namespace wrach

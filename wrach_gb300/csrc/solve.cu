@@ -324,7 +324,8 @@ cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st) {
 
 uint32_t solve_blocks(const SolveArgs& a) {
   const uint32_t threads = a.block ? a.block : 128;
-  const uint32_t blocks = (a.n + threads - 1) / threads;
+  const uint32_t per = a.per_thread ? a.per_thread : 1u;
+  const uint32_t blocks = (a.n + threads * per - 1) / (threads * per);
   // a launch that usually returns at once (the surrogate's fallback) strides
   // over the frame with a few blocks per SM, so that skipping it is cheap
   const uint32_t few = (uint32_t)(a.sms > 0 ? a.sms : 1) * (1024u / threads);

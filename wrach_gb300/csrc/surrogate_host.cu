@@ -77,7 +77,7 @@ int enqueue_rebin(WrachContext* ctx) {
   r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
   r.force_general = 0;
   CK(wrach::launch_count_sort(r, ctx->big_blocks, ctx->stream));
-  ctx->launches += wrach::count_sort_launches(r.n);
+  ctx->launches += wrach::count_sort_launches(r.n, ctx->ncells);
   ctx->cur ^= 1;
   return WRACH_OK;
 }

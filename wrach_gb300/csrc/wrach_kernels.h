@@ -23,6 +23,7 @@ struct SolveArgs {
   uint32_t* keys;               // next cell of each output particle
   Ctrl* ctrl;
   uint32_t block;               // threads per block of the solve kernels (<= 512)
+  uint32_t per_thread;          // extended solve: particles per thread in turn (0 = 1)
   const uint32_t* run_if;       // extended solve: skip the launch when *run_if == 0 (optional)
   float* part;                  // final extended pass: per-block metrics, 8 floats a block (optional)
   CountDev count;               // final extended pass: take the rebin's tickets (count.ticket set)
@@ -87,6 +88,7 @@ struct RebinArgs {
   float2* tp_pos;               // compacted positions
   float2* tp_vel;               // compacted velocities
   uint32_t* tp_cell;            // compacted cells
+  uint32_t tiles_prefixed;      // scan step: tile sums already turned into prefixes (set by it)
 };
 
 constexpr uint32_t kRebinThreads = 256;
@@ -122,7 +124,11 @@ cudaError_t launch_count_sort(const RebinArgs& a, uint32_t big_blocks, cudaStrea
 constexpr int kCountSortSteps = 5;
 cudaError_t launch_count_sort_step(const RebinArgs& a, int step, uint32_t big_blocks,
                                    cudaStream_t st, bool* launched);
-uint32_t count_sort_launches(uint32_t n);
+// Steps of one rebin (count, scan, scatter, place, large cells; the scan
+// alone when there are no particles) and its kernel launches (a large grid's
+// scan step is two launches).
+uint32_t count_sort_steps(uint32_t n);
+uint32_t count_sort_launches(uint32_t n, uint32_t ncells);
 
 // Keys for an upload re-pack: the first n_keep sources are particles of the
 // current frame (their cell, or `ncells` if they belong to world `target`),
