@@ -194,18 +194,17 @@ def oracle_setup(dims, pos, vel, cfg):
 def cpu_frames(dims, pos, vel, cfg, frames, seconds):
     """The oracle (C port of the reference's shader crate), all host threads,
     stepping frames 1..k of the trajectory from the initial state: the same
-    frames as the GPU line's timed window, k = min(frames, what fits in about
-    `seconds`).  Returns (particle-steps/s, k, seconds taken, threads)."""
+    frames as the GPU line's timed window, k = frames, or fewer when the
+    steps (taken 10 frames at a time) pass about `seconds`.  Returns
+    (particle-steps/s, k, seconds taken, threads)."""
     O, w, ph, table, p, v = oracle_setup(dims, pos, vel, cfg)
-    t0 = time.perf_counter()
-    table, p, v, _ = O.step(w, ph, table, p, v, 1)
-    one = time.perf_counter() - t0
-    k = max(1, min(frames, int(seconds / max(one, 1e-6))))
-    dt = one
-    if k > 1:
+    k, dt = 0, 0.0
+    while k < frames and (k == 0 or dt < seconds):
+        chunk = min(10, frames - k)
         t0 = time.perf_counter()
-        O.step(w, ph, table, p, v, k - 1)
+        table, p, v, _ = O.step(w, ph, table, p, v, chunk)
         dt += time.perf_counter() - t0
+        k += chunk
     return len(pos) * k / dt, k, dt, O.num_threads()
 
 
@@ -593,6 +592,21 @@ def run_surrogate(args):
     sur_s, st = timed(lambda: sim.surrogate_step(frames, 0.2, 0.01))
     pen_sur = sim.frame_metrics()
     clocks.stop()
+    # the error bounds over time: both runs again from the initial state in
+    # chunks of 32 frames (one calibration frame and 31 gated surrogate frames
+    # each, as in one run), the overlap and kinetic energy sampled after each
+    # chunk and averaged over the last 10 samples (frames 705-1024)
+    samples = {"plain": [], "surrogate": []}
+    for name, fn in (("plain", lambda: sim.step(32)),
+                     ("surrogate", lambda: sim.surrogate_step(32, 0.2, 0.01))):
+        sim.set_particles(pos, vel)
+        for _ in range(32):
+            fn()
+            samples[name].append(sim.frame_metrics())
+    late = {k: np.array(v[-10:]) for k, v in samples.items()}
+    quality = {"frames": 1024, "sampled_every": 32, "averaged_over": "the last 10 samples",
+               "excess_mean_overlap_px": float(late["surrogate"][:, 0].mean() - late["plain"][:, 0].mean()),
+               "kinetic_energy_ratio": float(late["surrogate"][:, 2].mean() / late["plain"][:, 2].mean())}
     line = {"metric": "particle-steps/s at 1M particles, surrogate frames (gated) vs plain frames",
             "value": n * frames / sur_s, "unit": "particle-steps/s", "n_gpus": 1, "steps": frames,
             "higher_is_better": True, "dtype": "bf16 network / f32 physics", "data": "synthetic",
@@ -622,6 +636,7 @@ def run_surrogate(args):
                                  "mma_sync": {"kernel": "k_mlp_forward", "ms": 1000 * mma_s,
                                               "achieved": flop_per_particle * n / mma_s / 1e12,
                                               "frac": flop_per_particle * n / mma_s / 1e12 / bf16_peak}},
+            "error_bounds_over_time": quality,
             "final_frame": {"plain_mean_penetration_px": pen_plain[0],
                             "surrogate_mean_penetration_px": pen_sur[0],
                             "excess_penetration_px": pen_sur[0] - pen_plain[0],
