@@ -158,7 +158,7 @@ def test_determinism(W):
     assert same_bits(out[0][0], out[1][0]) and same_bits(out[0][1], out[1][1])
 
 
-def test_capacity_error_keeps_state(W):
+def test_capacity_error_keeps_state(W, O):
     sim = make_sim(W, (20.0, 20.0), 1, capacity=100)
     try:
         pos, vel = _field(9, 80, (20.0, 20.0), 0.5)
@@ -168,6 +168,18 @@ def test_capacity_error_keeps_state(W):
             sim.add_particles(*_field(10, 30, (20.0, 20.0), 0.5))
         after = sim.read_frame()
         assert np.array_equal(before[2], after[2]) and same_bits(before[0], after[0])
+        # a replacing upload of more particles than the frame holds: refused
+        # when more than the capacity fall inside the grid, the frame kept ...
+        with pytest.raises(W.CapacityError):
+            sim.set_particles(*_field(11, 130, (20.0, 20.0), 0.5))
+        after = sim.read_frame()
+        assert np.array_equal(before[2], after[2]) and same_bits(before[0], after[0])
+        # ... and packed when no more than the capacity do
+        pos, vel = _field(12, 130, (20.0, 20.0), 0.5)
+        pos[:40] += np.float32(50.0)
+        sim.set_particles(pos, vel)
+        ref = O.pack(O.world(20.0, 20.0, 1), pos, vel, capacity=100)
+        assert_frame_equal(sim.read_frame(), ref, "130 particles, 90 inside")
     finally:
         sim.close()
 
@@ -257,6 +269,45 @@ def test_full_size_lattice_steps(W, O, mode):
     dims, pos, vel = workloads.lattice()
     _run_both(W, O, dims, 1, pos, vel, mode, [1, 2, 10], iterations=4,
               gravity=0.1 if mode else 0.0)
+
+
+def test_host_round_trip_frames_at_full_size(W, O):
+    """The end-to-end loop of a host application at the benchmark size:
+    each frame re-uploads the host's particles (pinned arrays), steps once
+    and reads the frame back into pinned arrays.  The upload copies the
+    velocities beside the positions' sort and returns before its last sort
+    steps end; every frame must still equal the oracle's."""
+    torch = pytest.importorskip("torch")
+    from wrach_gb300 import workloads
+    dims, pos, vel = workloads.lattice()
+    n = len(pos)
+    sim = make_sim(W, dims, 1, 1, 4, 0.1)
+    try:
+        cap, cells = sim.capacity(), sim.cells()
+        w = O.world(dims[0], dims[1], 1)
+        ph = oracle_physics(O, 1, 4, 0.1)
+        h_pos = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
+        h_vel = torch.empty((n, 2), dtype=torch.float32, pin_memory=True).numpy()
+        o_pos = torch.empty((cap, 2), dtype=torch.float32, pin_memory=True).numpy()
+        o_vel = torch.empty((cap, 2), dtype=torch.float32, pin_memory=True).numpy()
+        o_idx = torch.empty(cells + 2, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+        cur_pos, cur_vel = pos, vel
+        for frame in range(3):
+            h_pos[:len(cur_pos)] = cur_pos
+            h_vel[:len(cur_vel)] = cur_vel
+            sim.set_particles(h_pos[:len(cur_pos)], h_vel[:len(cur_vel)])
+            # the host arrays are free once the upload returns
+            h_pos[:] = np.nan
+            h_vel[:] = np.nan
+            sim.step(1)
+            sim.read(out=(o_pos, o_vel, o_idx))
+            m = int(o_idx[-1])
+            table, ref_pos, ref_vel = O.pack(w, cur_pos, cur_vel, capacity=cap)
+            ref = O.step(w, ph, table, ref_pos, ref_vel, 1)[:3]
+            assert_frame_equal((o_pos[:m], o_vel[:m], o_idx), ref, "round trip %d" % frame)
+            cur_pos, cur_vel = o_pos[:m].copy(), o_vel[:m].copy()
+    finally:
+        sim.close()
 
 
 def test_clustered_blobs_checked_every_100_steps(W, O):

@@ -117,8 +117,10 @@ void release(WrachContext* ctx) {
     dfree(s.pos);
     dfree(s.vel);
   }
+  if (ctx->gather_h) cudaFreeHost(ctx->gather_h);
   if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
   if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
+  if (ctx->counts_ev) cudaEventDestroy(ctx->counts_ev);
   if (ctx->aux) cudaStreamDestroy(ctx->aux);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
 }
@@ -484,6 +486,7 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   if ((e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking)) != cudaSuccess) return oom(e);
   if ((e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming)) != cudaSuccess) return oom(e);
   if ((e = cudaEventCreateWithFlags(&ctx->join_ev, cudaEventDisableTiming)) != cudaSuccess) return oom(e);
+  if ((e = cudaEventCreateWithFlags(&ctx->counts_ev, cudaEventDisableTiming)) != cudaSuccess) return oom(e);
   const size_t tc = ctx->total_cap;
   // the worlds, then (batches) the first world of each tile of cells
   const size_t tiles_words = nworlds > 1 ? (size_t)wrach::world_tiles(ctx->ncells) + 2 : 0;
@@ -535,6 +538,9 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
   if ((e = cudaMemset(ctx->counts, 0, ((size_t)ctx->ncells + 1) * 4)) != cudaSuccess) return oom(e);
   if ((e = dalloc(&ctx->gather_idx, nworlds + 1)) != cudaSuccess) return oom(e);
   if ((e = dalloc(&ctx->gather_out, nworlds + 1)) != cudaSuccess) return oom(e);
+  if ((e = cudaMallocHost(reinterpret_cast<void**>(&ctx->gather_h), (nworlds + 1) * sizeof(uint32_t))) !=
+      cudaSuccess)
+    return oom(e);
   {
     std::vector<uint32_t> idx(nworlds + 1);
     for (uint32_t w = 0; w < nworlds; ++w) idx[w] = ctx->worlds_h[w].cell_off;
@@ -580,9 +586,23 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
   if (replace) s.n = 0;
   int rc = ensure_store(ctx, s, (size_t)s.n + n_add);
   if (rc) return rc;
+  // One world re-packed from a store that holds no more particles than its
+  // frame: the capacity check below cannot fail, so the sort places straight
+  // into the frame buffers, and the velocities are copied on the second
+  // stream while the positions' keys are counted, scanned and scattered
+  // (only the place steps read them).
+  const bool direct = ctx->nworlds == 1 && replace && n_add <= ctx->cap_h[world];
+  const bool vel_aside = direct && n_add;
   if (n_add) {
     CK(cudaMemcpyAsync(s.pos + s.n, pos, (size_t)n_add * sizeof(float2), kind, ctx->stream));
-    CK(cudaMemcpyAsync(s.vel + s.n, vel, (size_t)n_add * sizeof(float2), kind, ctx->stream));
+    if (vel_aside) {
+      CK(cudaEventRecord(ctx->fork_ev, ctx->stream));
+      CK(cudaStreamWaitEvent(ctx->aux, ctx->fork_ev, 0));
+      CK(cudaMemcpyAsync(s.vel + s.n, vel, (size_t)n_add * sizeof(float2), kind, ctx->aux));
+      CK(cudaEventRecord(ctx->join_ev, ctx->aux));
+    } else {
+      CK(cudaMemcpyAsync(s.vel + s.n, vel, (size_t)n_add * sizeof(float2), kind, ctx->stream));
+    }
   }
   s.n += n_add;
 
@@ -619,22 +639,39 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
   r.pos_src = src_pos;
   r.vel_src = src_vel;
   r.cs_new = ctx->cs[ctx->cur ^ 1];
-  r.pos_dst = ctx->pos_o;
-  r.vel_dst = ctx->vel_o;
+  r.pos_dst = direct ? ctx->pos : ctx->pos_o;
+  r.vel_dst = direct ? ctx->vel : ctx->vel_o;
   r.cell_dst = ctx->cell_of[ctx->cur ^ 1];
   r.force_general = 1;
-  CK(wrach::launch_count_sort(r, ctx->big_blocks, ctx->stream));
-  ctx->launches += wrach::count_sort_launches(r.n, ctx->ncells);
-
-  // per-world counts from the new table
+  // per-world counts from the new table, read back as soon as the scan has
+  // written it
   const uint32_t nw = ctx->nworlds;
-  k_gather_u32<<<(nw + 1 + 255) / 256, 256, 0, ctx->stream>>>(ctx->cs[ctx->cur ^ 1], ctx->gather_idx,
-                                                               nw + 1, ctx->gather_out);
-  CK(cudaGetLastError());
-  ctx->launches += 1;
-  std::vector<uint32_t> starts(nw + 1);
-  CK(cudaMemcpyAsync(starts.data(), ctx->gather_out, (nw + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+  for (int step = 0; step < wrach::kCountSortSteps; ++step) {
+    // the place steps (3, 4) are the first to read the velocities
+    if (vel_aside && step == 3) CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0));
+    bool launched;
+    CK(wrach::launch_count_sort_step(r, step, ctx->big_blocks, ctx->stream, &launched));
+    if (step == 1) {
+      k_gather_u32<<<(nw + 1 + 255) / 256, 256, 0, ctx->stream>>>(ctx->cs[ctx->cur ^ 1],
+                                                                   ctx->gather_idx, nw + 1,
+                                                                   ctx->gather_out);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(ctx->gather_h, ctx->gather_out, (nw + 1) * 4, cudaMemcpyDeviceToHost,
+                         ctx->stream));
+      CK(cudaEventRecord(ctx->counts_ev, ctx->stream));
+    }
+  }
+  ctx->launches += wrach::count_sort_launches(r.n, ctx->ncells) + 1;
+  if (direct) {
+    // the call returns once the counts are known and both host arrays have
+    // been read; the place steps are still running, ahead of whatever the
+    // caller enqueues next on the context's stream
+    CK(cudaEventSynchronize(ctx->counts_ev));
+    if (vel_aside) CK(cudaEventSynchronize(ctx->join_ev));
+  } else {
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  const std::vector<uint32_t> starts(ctx->gather_h, ctx->gather_h + nw + 1);
   for (uint32_t w = 0; w < nw; ++w) {
     const uint32_t cnt = starts[w + 1] - starts[w];
     if (cnt > ctx->cap_h[w]) {
@@ -645,7 +682,7 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
     }
   }
   const uint32_t total = starts[nw];
-  if (total) {
+  if (total && !direct) {
     CK(cudaMemcpyAsync(ctx->pos, ctx->pos_o, (size_t)total * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->vel, ctx->vel_o, (size_t)total * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
   }
@@ -656,7 +693,7 @@ int upload_impl(WrachContext* ctx, uint32_t world, const float* pos,
     ctx->poff_h[w] = starts[w];
   }
   ctx->graph_ok = true;
-  CK(cudaStreamSynchronize(ctx->stream));
+  if (!direct) CK(cudaStreamSynchronize(ctx->stream));
   return WRACH_OK;
 }
 

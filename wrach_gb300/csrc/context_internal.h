@@ -30,6 +30,8 @@ struct WrachContext {
   // a frame's large-cell sort runs on `aux`, beside the small cells' pass
   cudaStream_t aux = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // uploads: the per-world counts read back (the call waits for them only)
+  cudaEvent_t counts_ev = nullptr;
   WrachConfig cfg{};
   wrach::PhysDev ph{};
   uint32_t nworlds = 0;
@@ -72,6 +74,7 @@ struct WrachContext {
   uint32_t* table_tmp = nullptr;  // one world's reference-layout table
   uint32_t* gather_idx = nullptr; // nworlds + 1
   uint32_t* gather_out = nullptr;
+  uint32_t* gather_h = nullptr;   // pinned host copy of gather_out (nworlds + 1)
   std::string err;
   uint64_t launches = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
