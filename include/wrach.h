@@ -121,7 +121,11 @@ int wrach_add_particles(WrachContext *ctx, uint32_t world, const float *pos,
 /* Replaces the world's store with these n particles and re-packs the frame
  * from them (ParticleStore::add_particles_to_cell followed by
  * create_packed_data, runners/bevy/src/particle_store.rs:62-65,103-149,
- * for the whole store at once). */
+ * for the whole store at once).  The host arrays are read before the call
+ * returns (pinned memory makes the copies faster).  With one world and no
+ * more particles than the frame capacity, the last steps of the re-pack may
+ * still be running on the context's stream when it returns; every later call
+ * on the context is ordered after them. */
 int wrach_set_particles(WrachContext *ctx, uint32_t world, const float *pos,
                         const float *vel, uint32_t n);
 
