@@ -84,6 +84,32 @@ def test_upload_empty_and_repack_store(W, O):
         sim.close()
 
 
+def test_replacing_uploads_empty_and_refilled(W, O):
+    # replacing uploads into the frame buffers directly: empty after a full
+    # frame, then refilled, each followed by frames that match the oracle
+    dims = (64.0, 48.0)
+    pos, vel = _field(13, 2500, dims, 1.0, outside=3.0)
+    sim = make_sim(W, dims, 1, 1, 4, 0.1)
+    try:
+        w, ph = O.world(*dims, 1), oracle_physics(O, 1, 4, 0.1)
+        sim.set_particles(pos, vel)
+        sim.step(3)
+        empty = np.zeros((0, 2), np.float32)
+        sim.set_particles(empty, empty)
+        p, v, t = sim.read_frame()
+        assert len(p) == 0 and not t.any()
+        sim.step(2)
+        assert len(sim.read_frame()[0]) == 0
+        sim.set_particles(pos[:1700], vel[:1700])
+        ref = O.pack(w, pos[:1700], vel[:1700], capacity=sim.capacity())
+        assert_frame_equal(sim.read_frame(), ref, "refilled")
+        sim.step(4)
+        ref = O.step(w, ph, ref[0], ref[1], ref[2], 4)[:3]
+        assert_frame_equal(sim.read_frame(), ref, "4 frames after the refill")
+    finally:
+        sim.close()
+
+
 @pytest.mark.parametrize("seed", [0, 1])
 def test_reference_mode_bit_exact(W, O, seed):
     # dense enough that cells overflow the capacity of 9 (cell.rs:79-95)

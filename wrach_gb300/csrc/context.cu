@@ -125,9 +125,14 @@ void release(WrachContext* ctx) {
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
 }
 
+// The buffers below may still be in use by work queued on the context's
+// streams (a frame, or the last steps of an upload), so a reallocation waits
+// for that work before freeing them.
 int ensure_sort_capacity(WrachContext* ctx, size_t need) {
   if (need <= ctx->sort_cap) return WRACH_OK;
   size_t cap = std::max(need, ctx->sort_cap * 2);
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaStreamSynchronize(ctx->aux));
   uint32_t** bufs[] = {&ctx->keys, &ctx->kA, &ctx->kB, &ctx->iA, &ctx->iB};
   for (auto b : bufs) {
     dfree(*b);
@@ -147,6 +152,8 @@ int ensure_sort_capacity(WrachContext* ctx, size_t need) {
 int ensure_stage(WrachContext* ctx, size_t need) {
   if (need <= ctx->stage_cap) return WRACH_OK;
   size_t cap = std::max(need, ctx->stage_cap * 2);
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaStreamSynchronize(ctx->aux));
   dfree(ctx->stage_pos);
   dfree(ctx->stage_vel);
   ctx->stage_pos = ctx->stage_vel = nullptr;
@@ -166,8 +173,9 @@ int ensure_store(WrachContext* ctx, Store& s, size_t need) {
   if (s.n) {
     CK(cudaMemcpyAsync(np, s.pos, s.n * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
     CK(cudaMemcpyAsync(nv, s.vel, s.n * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
   }
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaStreamSynchronize(ctx->aux));
   dfree(s.pos);
   dfree(s.vel);
   s.pos = np;
