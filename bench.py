@@ -16,7 +16,8 @@ walls, velocity clamp 1).  A step is one frame: solve + rebin.
            the device re-pack), runs one frame and reads the frame back
            (wrach_read: D2H of positions, velocities and the table)
   roofline the dominant kernel's algorithmic bytes / its mean CUDA-event
-           duration, against the measured HBM copy bandwidth
+           duration on eager frames sampled within the timed frames 1..K,
+           against the measured HBM copy bandwidth
 
 `--impl reference` times the reference's CPU path (the oracle port of the
 shader crate, all host threads) on the same workload and metric.
@@ -101,14 +102,16 @@ def _workload(name):
     return desc, dims, pos, vel, cfg
 
 
-def ncu_figure(workload_name, table, kernel):
+def ncu_figure(workload_name, table, kernel=None):
     """One figure of the committed ncu summary (profiles/ncu_traffic.json):
     `table` ("dram_bytes_per_launch" or "warp_instructions_per_launch") of
-    `kernel` in a capture of this very workload, or None when that workload
-    has no capture."""
+    `kernel` in a capture of this very workload (with no kernel: the entry
+    `table` itself, e.g. "frame", the captured frame), or None when that
+    workload has no capture."""
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            return json.load(f)["workloads"][workload_name][table].get(kernel)
+            entry = json.load(f)["workloads"][workload_name][table]
+        return entry if kernel is None else entry.get(kernel)
     except Exception:
         return None
 
@@ -256,9 +259,9 @@ def run_reference(args):
 
 
 # algorithmic bytes of each launch of a frame (n particles, c cells)
-def launch_bytes(kind, n, c):
-    if kind == "jacobi":
-        return 20 * n + 4 * c       # q in + q out + cell, capped table once (all take part)
+def launch_bytes(kind, n, c, n_tp=None):
+    if kind == "jacobi":            # over the n_tp taking-part particles (default: all)
+        return 20 * (n if n_tp is None else n_tp) + 4 * c  # q in + q out + cell, capped table once
     if kind == "jacobi_final":
         return 40 * n + 4 * c       # q, vel, cell_of in; pos, vel, key out
     if kind == "solve_reference":
@@ -268,7 +271,7 @@ def launch_bytes(kind, n, c):
     if kind == "rebin_count":
         return 8 * n                # keys in, tickets out
     if kind == "rebin_scan":
-        return 16 * c               # counts in and cleared, both tables out
+        return 12 * c               # counts in; cell-start and capped tables out
     if kind == "rebin_scatter":
         return 20 * n               # keys, tickets, starts in; source and cell out
     if kind == "rebin_place":
@@ -345,15 +348,23 @@ def run_ours(args):
     if len(traj) > 100:
         phases["frames_%d_%d_ms" % (len(traj) - 99, len(traj))] = float(traj[-100:].mean())
 
-    # per-kernel durations of eager frames sampled along the trajectory
+    # per-kernel durations of eager frames sampled over the timed window
+    # (frames 1..K of the trajectory), the frames the line's value covers
     solve_kinds = (["jacobi"] * (cfg["iterations"] - 1) + ["jacobi_final"] if cfg["mode"] else
                    ["solve_reference"])
     # extended frames take the rebin's tickets in their last Jacobi pass
     rebin_kinds = REBIN_STEPS[1:] if cfg["mode"] else REBIN_STEPS
     kinds = solve_kinds + ["rebin_" + s for s in rebin_kinds]
     sim.set_particles(pos, vel)
-    every = max(1, args.trajectory // max(1, args.profile_frames))
+    window = min(args.steps, args.trajectory)
+    every_prof = max(1, window // max(1, args.profile_frames))
+    every = max(1, args.trajectory // 10)
     prof, nprof = np.zeros(len(kinds)), 0
+    # the taking-part particles of the profiled frames (the first
+    # cell_capacity of each cell), whose compacted iterates the Jacobi
+    # launches read and write
+    cell_cap = W.WrachConfig().cell_capacity
+    n_tp = 0.0
     # states along the trajectory for the CPU baseline's trajectory-wide rate
     want_states = rank == 0 and world == 1 and not args.no_cpu_baseline
     states = []
@@ -361,13 +372,17 @@ def run_ours(args):
         if want_states and k % every == 0:
             p_k, v_k, t_k = sim.read_frame()
             states.append((k, t_k.copy(), p_k.copy(), v_k.copy()))
-        if k % every == every - 1:
+        if k < window and k % every_prof == every_prof - 1:
+            if cfg["mode"]:
+                counts = np.diff(sim.read_frame()[2][1:].astype(np.int64))
+                n_tp += float(np.minimum(counts, cell_cap).sum())
             flush_l2()
             prof += np.array(sim.profile_frame())
             nprof += 1
         else:
             sim.step(1)
     prof /= max(nprof, 1)
+    n_tp = n_tp / max(nprof, 1) if cfg["mode"] else float(n)
     per_kind = {}
     for k, ms in zip(solve_kinds, prof):
         per_kind.setdefault(k, []).append(ms)
@@ -380,10 +395,10 @@ def run_ours(args):
     per_kind["rebin"] = [float(sum(rebin_steps.values()))]
     dom_ms = statistics.mean(per_kind[dom])
     peak, peak_kind = measured_peak()
-    achieved = launch_bytes(dom, n, cells) / (dom_ms / 1000.0) / 1e9
+    achieved = launch_bytes(dom, n, cells, n_tp) / (dom_ms / 1000.0) / 1e9
     step_bytes = 32 * n + 8 * cells
     kernels = {k: {"launches_per_step": len(v), "mean_ms": statistics.mean(v),
-                   "gbs": launch_bytes(k, n, cells) / (statistics.mean(v) / 1000.0) / 1e9}
+                   "gbs": launch_bytes(k, n, cells, n_tp) / (statistics.mean(v) / 1000.0) / 1e9}
                for k, v in per_kind.items()}
 
     # end to end through the C ABI with pinned host buffers
@@ -420,9 +435,12 @@ def run_ours(args):
     # the Jacobi is bound by instruction issue: its warp instructions per
     # launch (one ncu capture of this workload) over its live mean duration,
     # against one instruction per scheduler per cycle on every SM
+    # (only when the timed window is the early frames around the captured
+    # one: the instruction count changes along the trajectory)
     issue = None
     inst = ncu_figure(desc["workload"], "warp_instructions_per_launch", dom)
-    if inst and clock_summary.get("sm_max_mhz"):
+    cap_frame = ncu_figure(desc["workload"], "frame")
+    if inst and cap_frame and cap_frame <= window <= 100 and clock_summary.get("sm_max_mhz"):
         sms = torch.cuda.get_device_properties(local).multi_processor_count
         ipeak = sms * 4 * clock_summary["sm_max_mhz"] * 1e6
         issue = {"kernel": dom, "warp_instructions_per_launch": inst,
@@ -447,8 +465,9 @@ def run_ours(args):
                      "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": ncu_figure(desc["workload"], "dram_bytes_per_launch", dom),
                      "traffic_source": "profiles/ncu_traffic.json (ncu dram__bytes_read+write, one launch"
-                                       " of this workload; null: no capture of it)",
-                     "algorithmic_bytes_per_launch": launch_bytes(dom, n, cells)},
+                                       " of this workload at frame %s; null: no capture of it)" % cap_frame,
+                     "algorithmic_bytes_per_launch": launch_bytes(dom, n, cells, n_tp),
+                     "taking_part_particles": n_tp},
         "step_roofline": {"algorithmic_bytes_per_step": step_bytes,
                           "achieved": step_bytes / (max_ms / args.steps / 1000.0) / 1e9,
                           "frac": step_bytes / (max_ms / args.steps / 1000.0) / 1e9 / peak},
