@@ -650,8 +650,9 @@ def run_surrogate(args):
                                  "unit": "TFLOP/s", "frac": net_tflops / bf16_peak,
                                  "flop_per_particle": flop_per_particle, "ms": 1000 * fwd_s,
                                  "note": "tcgen05.mma kind::f16 (M 128, N 64/64/16, K 64), BF16 operands in"
-                                         " shared memory, FP32 accumulators in TMEM; tanh-form GELU on"
-                                         " tanh.approx.f32",
+                                         " shared memory, FP32 accumulators in TMEM, two 128-row tiles"
+                                         " in flight per CTA; tanh-form GELU on packed FP16 pairs"
+                                         " (tanh.approx.f16x2)",
                                  "mma_sync": {"kernel": "k_mlp_forward", "ms": 1000 * mma_s,
                                               "achieved": flop_per_particle * n / mma_s / 1e12,
                                               "frac": flop_per_particle * n / mma_s / 1e12 / bf16_peak}},

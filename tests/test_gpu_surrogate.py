@@ -83,10 +83,12 @@ def test_forward_and_gradients_match_oracle(W):
             assert err < 3e-2, (name, err)
 
 
-@pytest.mark.parametrize("n", [1, 127, 128, 129, 70001])
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 70001, 400009])
 def test_tcgen05_forward_matches_mma_forward(W, n):
-    # the tcgen05 kernel (tiles of 128 rows, accumulators in tensor memory)
-    # against the mma.sync kernel on the same rows, ragged last tiles included
+    # the tcgen05 kernel (tiles of 128 rows in two slots per CTA, accumulators
+    # in tensor memory) against the mma.sync kernel on the same rows, ragged
+    # last tiles included; 400,009 rows give every CTA several tiles, so both
+    # slots and their refills run
     torch = _torch()
     rng = np.random.default_rng(7 + n)
     with _sim(W, (30.0, 30.0), 100) as sim:

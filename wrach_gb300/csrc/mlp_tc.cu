@@ -6,14 +6,18 @@
 // registers.
 //
 // One CTA of 256 threads takes tiles of 128 rows (M = 128), persistent over
-// the rows.  Per tile: the threads copy the tile's features into shared
-// memory; one thread issues the layer's tcgen05.mma (K = 64 as four K = 16
-// steps) and commits them to an mbarrier; the threads wait on it, read their
-// part of the accumulator from TMEM (tcgen05.ld: warp w reads TMEM lanes
-// 32 (w % 4) .. + 31, the tile's rows, and columns 32 (w / 4) .. + 31 of the
-// layer), add the bias, apply the GELU, round to BF16 and write them back
-// into the operand buffer for the next layer.  Several CTAs share an SM, so
-// one CTA's MMAs overlap the others' epilogues.
+// the rows, two tiles at a time in two slots, each with its own operand
+// buffer, 64 TMEM columns and mbarrier.  Per tile and layer: one thread
+// issues the layer's tcgen05.mma (K = 64 as four K = 16 steps) into the
+// slot's columns and commits them to the slot's mbarrier; the threads wait
+// on it, read their part of the accumulator from TMEM (tcgen05.ld: warp w
+// reads TMEM lanes 32 (w % 4) .. + 31, the tile's rows, and columns
+// 32 (w / 4) .. + 31 of the layer), add the bias, apply the GELU, round to
+// BF16 and write them back into the slot's operand buffer for the next
+// layer.  The slots alternate, so one tile's MMAs run while the threads work
+// on the other tile's epilogue; the next tiles' features are copied into the
+// freed buffers with cp.async while the outputs are written.  Several CTAs
+// share an SM as well.
 //
 // Shared-memory operands use the canonical K-major layout without swizzle:
 // 8-row x 16-byte core matrices, element (r, k) of a [rows][64] BF16 matrix at
@@ -38,7 +42,7 @@ namespace {
 
 constexpr uint32_t kTcRows = 128;     // M: rows per tile
 constexpr uint32_t kTcThreads = 256;  // two threads per row in the epilogues
-constexpr uint32_t kTcCols = 128;     // TMEM columns: D1 at 0..63, D2 at 64..127, D3 at 0..15
+constexpr uint32_t kTcCols = 128;     // TMEM columns: slot s's layers at 64 s .. 64 s + 63
 constexpr uint32_t kTcPerSm = 4;      // CTAs per SM: 4 x 128 columns = the SM's 512
 constexpr uint32_t kCoreRowBytes = 1024, kCoreKBytes = 128;
 
@@ -47,14 +51,15 @@ __host__ __device__ constexpr uint32_t cm_off(uint32_t r, uint32_t k) {
 }
 
 struct SmemTc {
-  uint8_t a[kTcRows * kMlpIn * 2];      // the tile: features, then activations
+  uint8_t a[2][kTcRows * kMlpIn * 2];   // per slot, its tile: features, then activations
   uint8_t w1[kMlpHidden * kMlpIn * 2];  // B operands, [out][in]
   uint8_t w2[kMlpHidden * kMlpHidden * 2];
   uint8_t w3[16 * kMlpHidden * 2];      // outputs 8..15 zero (N = 16)
-  float b1[kMlpHidden], b2[kMlpHidden], b3[kMlpOutPad];
-  uint64_t mbar;
+  alignas(16) float b1[kMlpHidden];
+  alignas(16) float b2[kMlpHidden];
+  float b3[kMlpOutPad];
+  uint64_t mbar[2];
   uint32_t tmem;
-  uint32_t failed;
 };
 // a dynamic size that lets at most kTcPerSm CTAs share an SM (TMEM columns)
 constexpr size_t kTcSmem = 56 * 1024;
@@ -154,13 +159,16 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bia
   {
     float v[32];
     tmem_ld32(taddr + h * 32, v);
+    const float4* b4 = reinterpret_cast<const float4*>(bias + h * 32);  // 16-byte aligned
 #pragma unroll
     for (uint32_t c = 0; c < 4; ++c) {
+      const float4 lo = b4[2 * c], hi = b4[2 * c + 1];
+      const float b[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
       uint32_t w[4];
 #pragma unroll
       for (uint32_t q = 0; q < 4; ++q) {
         const uint32_t k = c * 8 + 2 * q;
-        w[q] = gelu2_bf16(v[k] + bias[h * 32 + k], v[k + 1] + bias[h * 32 + k + 1]);
+        w[q] = gelu2_bf16(v[k] + b[2 * q], v[k + 1] + b[2 * q + 1]);
       }
       *reinterpret_cast<uint4*>(a + cm_off(row, h * 32 + c * 8)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
@@ -202,9 +210,9 @@ k_mlp_forward_tc(MlpDev m, const uint16_t* __restrict__ x, uint32_t n, float2* _
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s.mbar)) : "memory");
+    for (uint32_t q = 0; q < 2; ++q)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s.mbar[q])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    s.failed = 0u;
   }
   fence_async_smem();
   fence_before();
@@ -212,62 +220,116 @@ k_mlp_forward_tc(MlpDev m, const uint16_t* __restrict__ x, uint32_t n, float2* _
   fence_after();
   const uint32_t tmem = s.tmem;
   const uint32_t lane_base = tmem + (((warp & 3u) * 32u) << 16);  // this warp's 32 TMEM lanes
-  uint32_t phase = 0;
-  bool ok = true;
-  auto layer = [&](uint32_t d_col, const uint8_t* w, uint32_t nout) {
+  uint32_t phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};  // an MMA committed to the slot's mbarrier, not yet waited
+  bool failed = false;               // a wait of this thread gave up
+  // the layer of slot q: its operand buffer (written by every thread) made
+  // visible to the tensor cores, the slot's earlier TMEM reads finished; the
+  // barrier also tells every thread whether a wait gave up anywhere, in
+  // which case nothing is issued and the caller stops
+  auto issue = [&](uint32_t q, const uint8_t* w, uint32_t nout) {
     fence_async_smem();
     fence_before();
-    __syncthreads();
+    if (__syncthreads_or(failed ? 1 : 0)) return false;
     if (tid == 0) {
       fence_after();
-      mma_layer(tmem + d_col, s.a, w, idesc_bf16(kTcRows, nout), &s.mbar);
+      mma_layer(tmem + 64u * q, s.a[q], w, idesc_bf16(kTcRows, nout), &s.mbar[q]);
     }
-    const bool done = mbar_wait(&s.mbar, phase, kWaitLimitNs);
-    phase ^= 1u;
+    pending[q] = true;
+    return true;
+  };
+  // this thread's wait for slot q's MMA (no barrier: the next issue's
+  // barrier reports a wait that gave up; one that gave up keeps the slot's
+  // phase, so the last bounded wait before the TMEM is freed still waits
+  // for that MMA)
+  auto wait = [&](uint32_t q) {
+    if (mbar_wait(&s.mbar[q], phase[q], kWaitLimitNs)) {
+      phase[q] ^= 1u;
+      pending[q] = false;
+    } else {
+      failed = true;
+    }
     fence_after();
-    return __syncthreads_and(done ? 1 : 0) != 0;
   };
-  // a tile's features, 16-byte chunks with consecutive threads along a row:
-  // this thread's chunks are loaded into registers one tile ahead, so the
-  // loads of the next tile are in flight while this one computes
-  constexpr uint32_t kChunks = kTcRows * 8 / kTcThreads;
-  uint4 next[kChunks];
-  auto fetch = [&](uint32_t tile) {
+  // a tile's features, 16-byte chunks with consecutive threads along a row,
+  // into slot q's buffer by cp.async (rows past n are zero-filled)
+  auto load = [&](uint32_t q, uint32_t tile) {
 #pragma unroll
-    for (uint32_t u = 0; u < kChunks; ++u) {
+    for (uint32_t u = 0; u < kTcRows * 8 / kTcThreads; ++u) {
       const uint32_t i = tid + u * kTcThreads, grow = tile * kTcRows + (i >> 3);
-      next[u] = grow < n ? *reinterpret_cast<const uint4*>(x + (size_t)grow * kMlpIn + (i & 7u) * 8)
-                         : make_uint4(0u, 0u, 0u, 0u);
+      const bool in = grow < n;
+      const uint16_t* src = x + (size_t)(in ? grow : 0u) * kMlpIn + (i & 7u) * 8;
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
+                       smem_u32(s.a[q] + cm_off(i >> 3, (i & 7u) * 8))),
+                   "l"(src), "r"(in ? 16u : 0u)
+                   : "memory");
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
   };
-  fetch(blockIdx.x);
-  for (uint32_t tile = blockIdx.x; ok && tile * kTcRows < n; tile += gridDim.x) {
-#pragma unroll
-    for (uint32_t u = 0; u < kChunks; ++u) {
-      const uint32_t i = tid + u * kTcThreads;
-      *reinterpret_cast<uint4*>(s.a + cm_off(i >> 3, (i & 7u) * 8)) = next[u];
-    }
-    fetch(tile + gridDim.x);
-    if (!(ok = layer(0, s.w1, kMlpHidden))) break;
-    hidden_epilogue(lane_base + 0, s.b1, s.a, row_in_tile, half);
-    if (!(ok = layer(kMlpHidden, s.w2, kMlpHidden))) break;
-    hidden_epilogue(lane_base + kMlpHidden, s.b2, s.a, row_in_tile, half);
-    if (!(ok = layer(0, s.w3, 16))) break;
+  auto loaded = [&]() { asm volatile("cp.async.wait_all;" ::: "memory"); };
+  auto output = [&](uint32_t q, uint32_t tile) {
     const uint32_t row = tile * kTcRows + row_in_tile;
     if (half == 0) {
       float y0, y1;
-      tmem_ld2(lane_base + 0, y0, y1);
+      tmem_ld2(lane_base + 64u * q, y0, y1);
       if (row < n) y[row] = make_float2(y0 + s.b3[0], y1 + s.b3[1]);
     }
-    fence_before();
-    __syncthreads();  // the operand buffer and TMEM are free for the next tile
-    fence_after();
+  };
+  const uint32_t step = 2u * gridDim.x;
+  uint32_t t0 = blockIdx.x, t1 = blockIdx.x + gridDim.x;
+  bool has0 = t0 * kTcRows < n, has1 = t1 * kTcRows < n;  // has1 implies has0
+  bool ok = true;
+  if (has0) load(0, t0);
+  if (has1) load(1, t1);
+  loaded();
+  if (has0) ok = issue(0, s.w1, kMlpHidden);
+  if (ok && has1) ok = issue(1, s.w1, kMlpHidden);
+  while (ok && has0) {
+    wait(0);
+    hidden_epilogue(lane_base + 0u, s.b1, s.a[0], row_in_tile, half);
+    if (!(ok = issue(0, s.w2, kMlpHidden))) break;
+    if (has1) {
+      wait(1);
+      hidden_epilogue(lane_base + 64u, s.b1, s.a[1], row_in_tile, half);
+      if (!(ok = issue(1, s.w2, kMlpHidden))) break;
+    }
+    wait(0);
+    hidden_epilogue(lane_base + 0u, s.b2, s.a[0], row_in_tile, half);
+    if (!(ok = issue(0, s.w3, 16))) break;
+    if (has1) {
+      wait(1);
+      hidden_epilogue(lane_base + 64u, s.b2, s.a[1], row_in_tile, half);
+      if (!(ok = issue(1, s.w3, 16))) break;
+    }
+    // the last layers read their buffers: once each is done, its next
+    // tile's features are copied in while the outputs are written (a
+    // buffer whose wait gave up is left alone)
+    const uint32_t n0 = t0 + step, n1 = t1 + step;
+    const bool next0 = n0 * kTcRows < n, next1 = n1 * kTcRows < n;
+    wait(0);
+    if (next0 && !failed) load(0, n0);
+    output(0, t0);
+    if (has1) {
+      wait(1);
+      if (next1 && !failed) load(1, n1);
+      output(1, t1);
+    }
+    loaded();
+    t0 = n0;
+    t1 = n1;
+    has0 = next0;
+    has1 = next1;
+    if (has0) ok = issue(0, s.w1, kMlpHidden);
+    if (ok && has1) ok = issue(1, s.w1, kMlpHidden);
   }
+  loaded();
+  ok = __syncthreads_or(failed ? 1 : 0) == 0;
   if (!ok) {
     // a wait gave up: report it, give the MMAs in flight one more bounded
     // wait, then free the TMEM
     if (tid == 0) atomicOr(flags, kFlagTimeout);
-    mbar_wait(&s.mbar, phase, kWaitLimitNs);
+    for (uint32_t q = 0; q < 2; ++q)
+      if (pending[q]) mbar_wait(&s.mbar[q], phase[q], kWaitLimitNs);
   }
   fence_before();
   __syncthreads();
