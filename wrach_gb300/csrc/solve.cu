@@ -130,20 +130,21 @@ __device__ __forceinline__ void tp_push(const WorldDev& w, const PhysDev& ph,
     rs[r] = ok ? ct[rb + x0] : 0u;
     re[r] = ok ? ct[rb + x1 + 1] : 0u;
   }
-  // the candidates within reach, two per step (an odd last step tests its
-  // one candidate twice and keeps the first result); a NaN distance counts as
-  // within reach, as in the reference's test
+  // the candidates within reach, three per step (a short last step tests
+  // its last candidate again and keeps the first result); a NaN distance
+  // counts as within reach, as in the reference's test
   Mask rmask[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     Mask close = 0;
     const uint32_t s0 = rs[r], e = re[r];
-    for (uint32_t j = s0; j < e; j += 2) {
-      const uint32_t j1 = min(j + 1, e - 1);
-      const f32x2 da = f2_sub(q[j], qi2), db = f2_sub(q[j1], qi2);
+    for (uint32_t j = s0; j < e; j += 3) {
+      const uint32_t j1 = min(j + 1, e - 1), j2 = min(j + 2, e - 1);
+      const f32x2 da = f2_sub(q[j], qi2), db = f2_sub(q[j1], qi2), dc = f2_sub(q[j2], qi2);
       const bool ca = !(f2_len2(da) >= ph.skip_d2);
       const bool cb = j + 1 < e && !(f2_len2(db) >= ph.skip_d2);
-      close |= (Mask)((ca ? 1u : 0u) | (cb ? 2u : 0u)) << (j - s0);
+      const bool cc = j + 2 < e && !(f2_len2(dc) >= ph.skip_d2);
+      close |= (Mask)((ca ? 1u : 0u) | (cb ? 2u : 0u) | (cc ? 4u : 0u)) << (j - s0);
     }
     // the particle itself (in the middle row) is not its own neighbour
     if (r == 1) close &= ~((Mask)1 << (t - s0));
