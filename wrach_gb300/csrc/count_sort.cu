@@ -303,9 +303,30 @@ __global__ void __launch_bounds__(256) k_cs_place(RebinArgs a) {
   if (k < a.ncells && c1 - c0 <= kSmallCell) {
     const uint32_t s1 = min(c1, min(total, a.n));
     const uint32_t me = a.idx_tmp[q];
+    // the particle's data and its cell's compacted start do not depend on
+    // its rank: their loads go out before the rank's
+    const bool src_ok = me < a.n;
+    const float2 p = src_ok ? a.pos_src[me] : make_float2(0.f, 0.f);
+    const float2 v = src_ok ? a.vel_src[me] : make_float2(0.f, 0.f);
+    const uint32_t tp0 = a.tp_cap ? a.ct_new[k] : 0u;
     uint32_t rank = 0;
     for (uint32_t m = c0; m < s1; ++m) rank += a.idx_tmp[m] < me ? 1u : 0u;
-    place_one(a, c0 + rank, rank, me, k, overflow);
+    const uint32_t slot = c0 + rank;
+    if (slot < a.dst_capacity && src_ok) {
+      a.pos_dst[slot] = p;
+      a.vel_dst[slot] = v;
+      a.cell_dst[slot] = k;
+      if (rank < a.tp_cap) {
+        const uint32_t t = tp0 + rank;
+        if (t < a.dst_capacity) {  // always true unless the scan timed out
+          a.tp_pos[t] = p;
+          a.tp_vel[t] = v;
+          a.tp_cell[t] = k;
+        }
+      }
+    } else {
+      ++overflow;
+    }
     // the scan has read the cell's count: zero for the next rebin (only
     // non-empty cells were counted)
     if (rank == 0) a.counts[k] = 0u;
