@@ -9,6 +9,7 @@
 //   pos, vel          binned state, float2 x capacity        (cell order)
 //   pos_o, vel_o      solve output, float2 x capacity        (same order)
 //   q1, q2            extended-mode Jacobi iterates
+//   rows              the iterations' neighbour-row ranges per compacted particle (4 planes)
 //   cell_of[2]        cell of each binned particle (u32)
 //   cs[2]             cell-start table, cells + 1 u32 (ping-pong per frame)
 //   ct[2], tp_pos[2], tp_vel[2], tp_cell[2]
@@ -105,7 +106,7 @@ void release(WrachContext* ctx) {
     for (void* p : sp) dfree(p);
   }
   void* ptrs[] = {ctx->worlds_d, ctx->pos, ctx->vel, ctx->pos_o, ctx->vel_o,
-                  ctx->q1, ctx->q2, ctx->cell_of[0], ctx->cell_of[1],
+                  ctx->q1, ctx->q2, ctx->rows, ctx->cell_of[0], ctx->cell_of[1],
                   ctx->cs[0], ctx->cs[1], ctx->keys, ctx->kA, ctx->kB,
                   ctx->iA, ctx->iB, ctx->tile_sums, ctx->ctrl, ctx->big_list,
                   ctx->ct[0], ctx->ct[1], ctx->tp_pos[0], ctx->tp_pos[1], ctx->tp_cell[0],
@@ -220,6 +221,8 @@ wrach::SolveArgs solve_args(WrachContext* ctx) {
   a.tp_pos = ctx->tp_pos[ctx->cur];
   a.tp_vel = ctx->tp_vel[ctx->cur];
   a.sms = ctx->sms;
+  a.rows = ctx->rows;
+  a.rows_stride = ctx->total_cap;
   return a;
 }
 
@@ -512,6 +515,8 @@ int create_impl(const WrachConfig* config, uint32_t nworlds, const float* dims,
     if ((e = dalloc(&ctx->q1, tc)) != cudaSuccess) return oom(e);
     if ((e = dalloc(&ctx->q2, tc)) != cudaSuccess) return oom(e);
   }
+  if (c.mode == WRACH_MODE_EXTENDED && ctx->ph.iterations >= 3)
+    if ((e = dalloc(&ctx->rows, 4 * tc)) != cudaSuccess) return oom(e);
   if (c.mode == WRACH_MODE_EXTENDED) {
     for (int i = 0; i < 2; ++i) {
       if ((e = dalloc(&ctx->ct[i], (size_t)ctx->ncells + 1)) != cudaSuccess) return oom(e);

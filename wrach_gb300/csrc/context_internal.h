@@ -46,6 +46,7 @@ struct WrachContext {
   wrach::WorldDev* worlds_d = nullptr;
   float2 *pos = nullptr, *vel = nullptr, *pos_o = nullptr, *vel_o = nullptr;
   float2 *q1 = nullptr, *q2 = nullptr;
+  uint32_t* rows = nullptr;  // the iterations' neighbour rows: 4 planes of total_cap u32
   uint32_t* cell_of[2] = {nullptr, nullptr};
   uint32_t* cs[2] = {nullptr, nullptr};
   int cur = 0;
@@ -154,7 +155,11 @@ cudaError_t enqueue_iterations(WrachContext* ctx, const wrach::SolveArgs& a, uin
   const float2* src = a.tp_pos;
   for (uint32_t it = 0; it < count; ++it) {
     float2* dst = (it & 1) ? ctx->q2 : ctx->q1;
-    const cudaError_t e = wrach::launch_jacobi_iteration(a, src, dst, st);
+    // the first iteration writes the particles' neighbour rows, the later
+    // ones read them
+    wrach::SolveArgs ai = a;
+    ai.rows_mode = count > 1 ? (it == 0 ? 1 : 2) : 0;
+    const cudaError_t e = wrach::launch_jacobi_iteration(ai, src, dst, st);
     if (e != cudaSuccess) return e;
     after();
     src = dst;

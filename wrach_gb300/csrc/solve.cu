@@ -111,17 +111,14 @@ __device__ __forceinline__ uint32_t low_bit(uint64_t m) { return __ffsll((long l
 // over the compacted iterate q.  Mask holds one bit per candidate of a row:
 // 3 * cap bits.  METRICS: pen = the deepest overlap min_d - distance with a
 // pushing neighbour.
-template <typename Mask, bool METRICS>
-__device__ __forceinline__ void tp_push(const WorldDev& w, const PhysDev& ph,
-                                        const uint32_t* __restrict__ ct,
-                                        const f32x2* __restrict__ q, f32x2 qi2, uint32_t c,
-                                        uint32_t t, float& ax, float& ay, float& pen) {
+// The compacted ranges [rs[r], re[r]) of the three neighbour rows of cell c
+// (independent loads of the capped table).
+__device__ __forceinline__ void tp_rows(const WorldDev& w, const uint32_t* __restrict__ ct,
+                                        uint32_t c, uint32_t (&rs)[3], uint32_t (&re)[3]) {
   uint32_t cx, cy;
   cell_xy(w, c - w.cell_off, cx, cy);
   const uint32_t x0 = cx > 0 ? cx - 1 : 0;
   const uint32_t x1 = cx + 1 < w.gx ? cx + 1 : w.gx - 1;
-  // the rows' compacted ranges first: independent loads
-  uint32_t rs[3], re[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     const int ny = (int)cy - 1 + r;
@@ -130,6 +127,15 @@ __device__ __forceinline__ void tp_push(const WorldDev& w, const PhysDev& ph,
     rs[r] = ok ? ct[rb + x0] : 0u;
     re[r] = ok ? ct[rb + x1 + 1] : 0u;
   }
+}
+
+// The push sum over the candidates of the rows [rs[r], re[r]) of the
+// compacted particle t (in the middle row).
+template <typename Mask, bool METRICS>
+__device__ __forceinline__ void tp_push_rows(const PhysDev& ph, const f32x2* __restrict__ q,
+                                             f32x2 qi2, uint32_t t, const uint32_t (&rs)[3],
+                                             const uint32_t (&re)[3], float& ax, float& ay,
+                                             float& pen) {
   // the candidates within reach, three per step (a short last step tests
   // its last candidate again and keeps the first result); a NaN distance
   // counts as within reach, as in the reference's test
@@ -180,26 +186,55 @@ __device__ __forceinline__ void tp_push(const WorldDev& w, const PhysDev& ph,
   }
 }
 
+template <typename Mask, bool METRICS>
+__device__ __forceinline__ void tp_push(const WorldDev& w, const PhysDev& ph,
+                                        const uint32_t* __restrict__ ct,
+                                        const f32x2* __restrict__ q, f32x2 qi2, uint32_t c,
+                                        uint32_t t, float& ax, float& ay, float& pen) {
+  uint32_t rs[3], re[3];
+  tp_rows(w, ct, c, rs, re);
+  tp_push_rows<Mask, METRICS>(ph, q, qi2, t, rs, re, ax, ay, pen);
+}
+
 // One Jacobi iteration but the last, one thread per compacted (taking-part)
 // particle: q' = q - push sum, over the compacted count ct[ncells] (a
 // grid-stride loop; the plain frames' grid covers every particle of the
 // frame, so each thread takes one or none).  A launch whose `run_if` flag
 // reads 0 returns at once.
-template <typename Mask>
+// ROWS 0: the neighbour rows from the capped table; 1: also written to
+// `rows` (4 planes of `stride`); 2: read from `rows` (the cell and its
+// world are then not needed).
+template <typename Mask, int ROWS>
 __global__ void __launch_bounds__(512)
 k_jacobi_tp(const WorldDev* __restrict__ worlds, int nworlds, PhysDev ph, uint32_t ncells,
             const uint32_t* __restrict__ ct, const uint32_t* __restrict__ tp_cell,
             const float2* __restrict__ qin, float2* __restrict__ qout,
-            const uint32_t* __restrict__ run_if) {
+            const uint32_t* __restrict__ run_if, uint32_t* __restrict__ rows, uint32_t stride) {
   if (run_if && *run_if == 0u) return;
   const uint32_t ntp = __ldg(ct + ncells);
   const f32x2* __restrict__ q = reinterpret_cast<const f32x2*>(qin);
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntp; t += gridDim.x * blockDim.x) {
-    const uint32_t c = tp_cell[t];
-    const WorldDev w = worlds[world_of_cell(worlds, nworlds, c)];
+    uint32_t rs[3], re[3];
+    if (ROWS == 2) {
+      const uint32_t len = rows[3 * (size_t)stride + t];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        rs[r] = rows[(size_t)r * stride + t];
+        re[r] = rs[r] + ((len >> (8 * r)) & 0xFFu);
+      }
+    } else {
+      const uint32_t c = tp_cell[t];
+      tp_rows(worlds[world_of_cell(worlds, nworlds, c)], ct, c, rs, re);
+      if (ROWS == 1) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) rows[(size_t)r * stride + t] = rs[r];
+        rows[3 * (size_t)stride + t] =
+            (re[0] - rs[0]) | ((re[1] - rs[1]) << 8) | ((re[2] - rs[2]) << 16);
+      }
+    }
     const f32x2 qi2 = q[t];
     float ax = 0.f, ay = 0.f, pen = 0.f;
-    tp_push<Mask, false>(w, ph, ct, q, qi2, c, t, ax, ay, pen);
+    tp_push_rows<Mask, false>(ph, q, qi2, t, rs, re, ax, ay, pen);
     qout[t] = make_float2(__fsub_rn(f2_x(qi2), ax), __fsub_rn(f2_y(qi2), ay));
   }
 }
@@ -338,12 +373,21 @@ cudaError_t launch_jacobi_iteration(const SolveArgs& a, const float2* qin, float
   if (a.n == 0) return cudaSuccess;
   const uint32_t threads = a.block ? a.block : 128;
   const uint32_t blocks = solve_blocks(a);
-  if (3 * a.ph.cap <= 32)
-    k_jacobi_tp<uint32_t><<<blocks, threads, 0, st>>>(a.worlds, a.nworlds, a.ph, a.ncells, a.ct,
-                                                       a.tp_cell, qin, qout, a.run_if);
-  else
-    k_jacobi_tp<uint64_t><<<blocks, threads, 0, st>>>(a.worlds, a.nworlds, a.ph, a.ncells, a.ct,
-                                                       a.tp_cell, qin, qout, a.run_if);
+  const int mode = a.rows ? a.rows_mode : 0;
+#define WRACH_TP(MASK, ROWS)                                                                  \
+  k_jacobi_tp<MASK, ROWS><<<blocks, threads, 0, st>>>(a.worlds, a.nworlds, a.ph, a.ncells, a.ct, \
+                                                      a.tp_cell, qin, qout, a.run_if, a.rows,  \
+                                                      a.rows_stride)
+  if (3 * a.ph.cap <= 32) {
+    if (mode == 1) WRACH_TP(uint32_t, 1);
+    else if (mode == 2) WRACH_TP(uint32_t, 2);
+    else WRACH_TP(uint32_t, 0);
+  } else {
+    if (mode == 1) WRACH_TP(uint64_t, 1);
+    else if (mode == 2) WRACH_TP(uint64_t, 2);
+    else WRACH_TP(uint64_t, 0);
+  }
+#undef WRACH_TP
   return cudaGetLastError();
 }
 

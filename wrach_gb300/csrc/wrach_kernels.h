@@ -33,6 +33,13 @@ struct SolveArgs {
   const float2* tp_pos;         // compacted positions of the binned state
   const float2* tp_vel;         // compacted velocities of the binned state
   int sms;                      // SMs of the device
+  // extended iterations (optional): each compacted taking-part particle's
+  // three neighbour rows, as 4 planes of rows_stride u32 (the rows' compacted
+  // starts, then their lengths packed one byte each); rows_mode 0 computes
+  // the rows from the capped table, 1 also writes them, 2 reads them
+  uint32_t* rows;
+  uint32_t rows_stride;
+  int rows_mode;
 };
 
 cudaError_t launch_solve_reference(const SolveArgs& a, cudaStream_t st);
